@@ -1,0 +1,225 @@
+/*
+ * meshode.h -- C ABI of libmeshode.so, the GB300 (sm_103a) implementation of
+ * MeshODE's per-iteration deformation hot path.
+ *
+ * Conventions
+ *   - Every entry point returns an int status (MO_OK == 0); on failure
+ *     mo_last_error() returns a message for the calling thread.
+ *   - Every pointer argument is a DEVICE pointer owned by the caller unless
+ *     the comment says "host".  `stream` is a cudaStream_t (NULL = legacy
+ *     default stream).  All calls are asynchronous on `stream` unless stated.
+ *   - Vertex arrays are float32 [n,3] row-major (the layout of the reference's
+ *     torch tensors); faces int32 [m,3]; edge lists int32 [k,2].
+ *   - Distance grids in MO_LAYOUT_LINEAR are float32 [N][N][N] indexed
+ *     [z][y][x] like UniformGrid::voxel_distance_ (src/lib/uniformgrid.h:33).
+ *   - The step path (loss, gradient, Adam, fused step) allocates nothing;
+ *     builders take caller scratch (or NULL: then the library allocates it
+ *     stream-ordered and frees it before returning).
+ */
+#ifndef MESHODE_GB300_H_
+#define MESHODE_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MO_OK 0
+#define MO_ERR_INVALID 1 /* bad argument (checked on the host) */
+#define MO_ERR_CUDA 2    /* CUDA runtime error */
+#define MO_ERR_SCRATCH 3 /* caller scratch too small */
+#define MO_ERR_DEVICE 4  /* a kernel reported an error through its status word */
+
+#define MO_LAYOUT_LINEAR 0 /* [z][y][x] float, 4*N^3 bytes */
+#define MO_LAYOUT_CELL 1   /* per cell (x,y,z < N-1) its 8 corners, 32 B = one sector */
+
+#define MO_DF_AUTO 0
+#define MO_DF_BRUTE 1 /* shared-memory-tiled brute force (small targets) */
+#define MO_DF_LBVH 2  /* Morton codes + radix sort + Karras LBVH + warp packet traversal */
+
+#define MO_EDGES_FACES 0 /* idx = F[m,3]; half-edge 3f+j = (F[f][j], F[f][(j+1)%3]) */
+#define MO_EDGES_LIST 1  /* idx = E[k,2]; edge k = (E[k][0], E[k][1]) */
+
+/* Message describing the last failure on this host thread. */
+const char* mo_last_error(void);
+/* Library ABI version (major*100 + minor). */
+int mo_version(void);
+
+/* ------------------------------------------------------------------------
+ * Normalisation by the target's transform.
+ * Replaces Mesh::Normalize (src/lib/mesh.cc:66-96), NormalizeByTemplate and
+ * DenormalizeByTemplate (src/interface/normalize.cc:5-45).
+ * ------------------------------------------------------------------------ */
+/* Exact per-axis min/max of V into bbox6 (device int32[6], ordered-int
+ * encoding: min x,y,z then max x,y,z).  NaNs are ignored. */
+int mo_bbox(const float* V, int64_t n, int32_t* bbox6, void* stream);
+/* params4 (device double[4]) = {scale, tx, ty, tz}:
+ * scale = 1.1 * longest extent, t = min - 0.05*scale (mesh.cc:79-82). */
+int mo_norm_params(const int32_t* bbox6, double* params4, void* stream);
+/* In place: v = (v - t)/scale (inverse == 0) or v = v*scale + t
+ * (inverse != 0), evaluated in double and rounded to float like
+ * normalize.cc:21 and :42. */
+int mo_normalize(float* V, int64_t n, const double* params4, int inverse, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Distance-field build.  Replaces Mesh::ConstructDistanceField
+ * (src/lib/mesh.cc:106-152) and its igl::point_mesh_squared_distance query
+ * (mesh.cc:140): grid[z][y][x] = unsigned distance from (x/N, y/N, z/N) to the
+ * nearest triangle of the target normalised by params4.
+ * ------------------------------------------------------------------------ */
+size_t mo_df_build_scratch_bytes(int64_t nv, int64_t nf, int N, int method);
+/* status_out: optional device int32.  When given, the call does not
+ * synchronise; bit 0 (a face index outside [0, nv)) and bit 1 (traversal
+ * stack overflow) are OR-ed into it for the caller to read later.  When NULL
+ * the call synchronises `stream` and reports those as MO_ERR_DEVICE. */
+int mo_df_build(const float* V, int64_t nv, const int32_t* F, int64_t nf, int N,
+                const double* params4, int method, void* scratch, size_t scratch_bytes,
+                float* grid_linear_out, int32_t* status_out, void* stream);
+/* The LBVH stages of mo_df_build on their own, for checking against a CPU
+ * build of the same codes: sorted 30-bit Morton codes of the triangle
+ * centroids (uint32[nf]), the stable sort permutation (int32[nf]), the Karras
+ * children of the nf-1 internal nodes (>= 0 internal, ~leaf for leaves) and
+ * the root box (float[6], lo then hi; for nf > 1).  Synchronises `stream`. */
+int mo_lbvh_build(const float* V, int64_t nv, const int32_t* F, int64_t nf, const double* params4,
+                  void* scratch, size_t scratch_bytes, uint32_t* sorted_codes, int32_t* order,
+                  int32_t* left, int32_t* right, float* root_box, void* stream);
+/* Method MO_DF_AUTO resolves to (host-side heuristic, exported for tests). */
+int mo_df_method_for(int64_t nf, int N);
+
+/* Bytes of a grid in `layout`; 0 for an invalid layout. */
+size_t mo_grid_bytes(int N, int layout);
+/* Re-lay a linear grid into `layout` (MO_LAYOUT_CELL packs each cell's 8
+ * corners contiguously so one trilinear lookup reads one 32-byte sector). */
+int mo_grid_relayout(const float* grid_linear, int N, int layout, float* out, void* stream);
+
+/* ------------------------------------------------------------------------
+ * DistanceFieldLoss.  Replaces DistanceFieldLoss_forward
+ * (src/interface/distance_layer.cc:8-37, per vertex d(v)^2 with
+ * UniformGrid::DistanceFloat, src/lib/uniformgrid.cc:120-185) and
+ * DistanceFieldLoss_backward (distance_layer.cc:39-81, d * grad d through
+ * ceres::Jet<float,3>).  Bit-identical to the reference's float arithmetic.
+ * ------------------------------------------------------------------------ */
+int mo_dfloss_forward(const float* V, int64_t n, const float* grid, int N, int layout,
+                      float* loss_out, void* stream);
+int mo_dfloss_backward(const float* V, int64_t n, const float* grid, int N, int layout,
+                       float* grad_out, void* stream);
+/* Both in one pass.  loss_out may be NULL.  If use_mask != 0 the gradient of
+ * vertex i is multiplied by (0.5*loss_i < mask_thresh), the d < 0.03 mask of
+ * GraphLossFunction (src/python/layers/graph_loss_layer.py:18,40). */
+int mo_dfloss_fwd_bwd(const float* V, int64_t n, const float* grid, int N, int layout,
+                      float* loss_out, float* grad_out, int use_mask, float mask_thresh,
+                      void* stream);
+
+/* ------------------------------------------------------------------------
+ * Edge (rigidity) losses.  Replaces StoreRigidityInformation /
+ * RigidEdgeLoss_forward / RigidEdgeLoss_backward (src/interface/rigid_layer.cc:
+ * 11-46, 48-89, 91-133) and StoreGraphInformation / GraphEdgeLoss_*
+ * (src/interface/graph_layer.cc:11-135).  The backward scatter is a
+ * deterministic per-vertex reduction over a vertex -> half-edge CSR whose
+ * entries are in half-edge order, which reproduces the reference's serial
+ * scatter bit for bit.
+ * ------------------------------------------------------------------------ */
+int64_t mo_edge_count(int64_t n_items, int kind);
+/* off_out [H,3] = v1 - v0 (rigid_layer.cc:29-45, graph_layer.cc:18-32). */
+int mo_edge_offsets(const float* V, int64_t nv, const int32_t* idx, int64_t n_items, int kind,
+                    float* off_out, void* stream);
+/* loss_out [H,3] = (v1 - v0 - off)^2 per component (rigid_layer.cc:72-86). */
+int mo_edge_forward(const float* V, int64_t nv, const int32_t* idx, int64_t n_items, int kind,
+                    const float* off, float* loss_out, void* stream);
+/* Bytes of the CSR buffer for nv vertices and the given half-edge list. */
+size_t mo_edge_csr_bytes(int64_t nv, int64_t n_items, int kind);
+/* Validates 0 <= index < nv on the device.  status_out: optional device
+ * int32; when given, the call does not synchronise and bit 0 is OR-ed into it
+ * for an out-of-range index.  When NULL the call synchronises `stream` and
+ * returns MO_ERR_DEVICE for an out-of-range index. */
+int mo_edge_csr_build(const int32_t* idx, int64_t n_items, int kind, int64_t nv, void* csr,
+                      size_t csr_bytes, int32_t* status_out, void* stream);
+/* grad_out [nv,3] = sum over incident half-edges of -/+ (v1 - v0 - off)
+ * (rigid_layer.cc:113-130). */
+int mo_edge_backward(const float* V, int64_t nv, const void* csr, int64_t nh, const float* off,
+                     float* grad_out, void* stream);
+
+/* Sliced-ELL (32-vertex slices, column-major records) view of the CSR for
+ * the fused step: records are float4 {other | role<<31, off.x, off.y, off.z},
+ * padding records have other == -1.  slice_ptr is int32[ceil(nv/32)+1];
+ * mo_sell_plan fills it asynchronously, the record count ending up in
+ * slice_ptr[ceil(nv/32)] (read it before sizing the records for
+ * mo_sell_fill). */
+int mo_sell_plan(const void* csr, int64_t nv, int64_t nh, int32_t* slice_ptr, void* stream);
+int mo_sell_fill(const void* csr, int64_t nv, int64_t nh, const float* off,
+                 const int32_t* slice_ptr, float* records, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Adam.  Replaces torch.optim.Adam([V], lr) in the reference's loops
+ * (src/python/rigid_deform.py:32,39): the update of
+ * torch/optim/adam.py _single_tensor_adam (lerp, mul/addcmul,
+ * sqrt/bias-correction, addcdiv) with step_size = lr/(1-b1^t) and
+ * bc2_sqrt = sqrt(1-b2^t) computed by the caller in double.
+ * ------------------------------------------------------------------------ */
+int mo_adam_step(float* P, const float* G, float* M, float* Vsq, int64_t n, float one_minus_b1,
+                 float b2, float one_minus_b2, float eps, float step_size, float bc2_sqrt,
+                 void* stream);
+
+/* ------------------------------------------------------------------------
+ * Fused optimiser step over many deformation pairs (serving).  One launch =
+ * one Adam step of every active pair: DF loss+gradient, edge residuals and
+ * their CSR-ordered gradient, optional mask/weights, Adam, and the per-tile
+ * loss partial.  Replaces the per-iteration body of rigid_deform.py:35-39 /
+ * cad_deform.py:30-35 (RigidLossFunction / GraphLossFunction + Adam).
+ * All descriptors live in device memory so a captured CUDA graph of these
+ * launches stays valid while pairs are admitted and retired.
+ * ------------------------------------------------------------------------ */
+typedef struct MoPair {
+    const float* grid;      /* layout-specific grid */
+    const int32_t* slice_ptr;
+    const float* sell;      /* float4 records */
+    float* pos0;            /* float4 [nv] positions, even steps read pos0 */
+    float* pos1;            /* float4 [nv] positions, odd steps read pos1 */
+    float* adam_m;          /* float [nv*3] */
+    float* adam_v;          /* float [nv*3] */
+    const float* adam_tab;  /* float2 [tmax]: (step_size, bc2_sqrt) of step t at index t-1 */
+    float* grad_dbg;        /* optional float [nv*3]: total gradient of each step */
+    int32_t N, layout, nv, nslices;
+    float w_edge;           /* edge-loss weight (1, lambda^2 or rigidity^2) */
+    float mask_thresh;      /* DF gradient mask threshold on 0.5*d^2 */
+    int32_t use_mask;
+    float grad_scale;       /* upstream gradient grad_h */
+    float one_minus_b1, b2, one_minus_b2, eps;
+    int32_t t0;             /* steps completed before this group of launches */
+    int32_t t_end;          /* last step to run */
+    int32_t tile0, ntiles;  /* the pair's contiguous range in the MoTile array */
+} MoPair;
+
+typedef struct MoTile {
+    int32_t pair;    /* index into the MoPair array */
+    int32_t slice0;  /* first 32-vertex slice of the tile */
+    int32_t nslices; /* 1..8 slices (one warp each) */
+    int32_t pad;
+} MoTile;
+
+/* One step (launch_index = 0.. within a group of launches; step t =
+ * t0 + launch_index + 1).  tile_loss[launch_index*max_tiles + tile] gets the
+ * tile's loss partial.  ntiles is read from device memory.  grid_ctas <= 0
+ * picks a persistent grid of resident CTAs. */
+int mo_fused_step(const MoPair* pairs, const MoTile* tiles, const int32_t* ntiles, int max_tiles,
+                  int launch_index, float* tile_loss, int grid_ctas, void* stream);
+/* pair_loss[k*npairs + p] (double) = sum, in tile order, of the tile
+ * partials of pair p (its MoPair tile0/ntiles range) for launches
+ * k = 0..nlaunch-1: the layer loss 0.5*sum d^2 + w_edge*0.5*sum |r|^2 at the
+ * positions before step t0+k+1. */
+int mo_pair_loss(const MoPair* pairs, int npairs, int max_tiles, int nlaunch, const float* tile_loss,
+                 double* pair_loss, void* stream);
+/* sizeof(MoPair) and sizeof(MoTile) as compiled (host pointers), so that
+ * bindings in other languages can check their struct layout. */
+int mo_abi_sizes(size_t* pair_bytes, size_t* tile_bytes);
+/* float [n,3] <-> float4 [n] position packing. */
+int mo_pack_pos(const float* V, int64_t n, float* pos4, void* stream);
+int mo_unpack_pos(const float* pos4, int64_t n, float* V, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MESHODE_GB300_H_ */

@@ -1,0 +1,128 @@
+"""ctypes binding of libmeshode.so (declared in include/meshode.h).
+
+The library is the only compute path: importing an entry point when the
+shared object is missing, or when no CUDA device is present, raises.
+"""
+import ctypes
+import os
+
+import torch
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libmeshode.so")
+
+MO_OK, MO_ERR_INVALID, MO_ERR_CUDA, MO_ERR_SCRATCH, MO_ERR_DEVICE = 0, 1, 2, 3, 4
+MO_LAYOUT_LINEAR, MO_LAYOUT_CELL = 0, 1
+MO_DF_AUTO, MO_DF_BRUTE, MO_DF_LBVH = 0, 1, 2
+MO_EDGES_FACES, MO_EDGES_LIST = 0, 1
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_I64 = ctypes.c_int64
+_F = ctypes.c_float
+_SZ = ctypes.c_size_t
+
+
+class MoPair(ctypes.Structure):
+    _fields_ = [
+        ("grid", _P), ("slice_ptr", _P), ("sell", _P), ("pos0", _P), ("pos1", _P),
+        ("adam_m", _P), ("adam_v", _P), ("adam_tab", _P), ("grad_dbg", _P),
+        ("N", ctypes.c_int32), ("layout", ctypes.c_int32), ("nv", ctypes.c_int32), ("nslices", ctypes.c_int32),
+        ("w_edge", _F), ("mask_thresh", _F), ("use_mask", ctypes.c_int32), ("grad_scale", _F),
+        ("one_minus_b1", _F), ("b2", _F), ("one_minus_b2", _F), ("eps", _F),
+        ("t0", ctypes.c_int32), ("t_end", ctypes.c_int32), ("tile0", ctypes.c_int32), ("ntiles", ctypes.c_int32),
+    ]
+
+
+class MoTile(ctypes.Structure):
+    _fields_ = [("pair", ctypes.c_int32), ("slice0", ctypes.c_int32), ("nslices", ctypes.c_int32),
+                ("pad", ctypes.c_int32)]
+
+
+# name -> (restype, argtypes)
+_SIGS = {
+    "mo_last_error": (ctypes.c_char_p, []),
+    "mo_version": (_I, []),
+    "mo_bbox": (_I, [_P, _I64, _P, _P]),
+    "mo_norm_params": (_I, [_P, _P, _P]),
+    "mo_normalize": (_I, [_P, _I64, _P, _I, _P]),
+    "mo_df_build_scratch_bytes": (_SZ, [_I64, _I64, _I, _I]),
+    "mo_df_build": (_I, [_P, _I64, _P, _I64, _I, _P, _I, _P, _SZ, _P, _P, _P]),
+    "mo_df_method_for": (_I, [_I64, _I]),
+    "mo_lbvh_build": (_I, [_P, _I64, _P, _I64, _P, _P, _SZ, _P, _P, _P, _P, _P, _P]),
+    "mo_grid_bytes": (_SZ, [_I, _I]),
+    "mo_grid_relayout": (_I, [_P, _I, _I, _P, _P]),
+    "mo_dfloss_forward": (_I, [_P, _I64, _P, _I, _I, _P, _P]),
+    "mo_dfloss_backward": (_I, [_P, _I64, _P, _I, _I, _P, _P]),
+    "mo_dfloss_fwd_bwd": (_I, [_P, _I64, _P, _I, _I, _P, _P, _I, _F, _P]),
+    "mo_edge_count": (_I64, [_I64, _I]),
+    "mo_edge_offsets": (_I, [_P, _I64, _P, _I64, _I, _P, _P]),
+    "mo_edge_forward": (_I, [_P, _I64, _P, _I64, _I, _P, _P, _P]),
+    "mo_edge_csr_bytes": (_SZ, [_I64, _I64, _I]),
+    "mo_edge_csr_build": (_I, [_P, _I64, _I, _I64, _P, _SZ, _P, _P]),
+    "mo_edge_backward": (_I, [_P, _I64, _P, _I64, _P, _P, _P]),
+    "mo_sell_plan": (_I, [_P, _I64, _I64, _P, _P]),
+    "mo_sell_fill": (_I, [_P, _I64, _I64, _P, _P, _P, _P]),
+    "mo_adam_step": (_I, [_P, _P, _P, _P, _I64, _F, _F, _F, _F, _F, _F, _P]),
+    "mo_fused_step": (_I, [_P, _P, _P, _I, _I, _P, _I, _P]),
+    "mo_pair_loss": (_I, [_P, _I, _I, _I, _P, _P, _P]),
+    "mo_abi_sizes": (_I, [ctypes.POINTER(_SZ), ctypes.POINTER(_SZ)]),
+    "mo_pack_pos": (_I, [_P, _I64, _P, _P]),
+    "mo_unpack_pos": (_I, [_P, _I64, _P, _P]),
+}
+
+_lib = None
+
+
+class MeshodeError(RuntimeError):
+    pass
+
+
+def lib():
+    """Load libmeshode.so once; raise if it is missing (no CPU fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise MeshodeError(
+                "libmeshode.so is not built (%s); run `python -c \"import __graft_entry__ as g; g.build()\"`"
+                % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def exported_symbols():
+    return sorted(_SIGS)
+
+
+def check(rc, what=""):
+    if rc != MO_OK:
+        msg = lib().mo_last_error()
+        msg = msg.decode() if msg else ""
+        raise MeshodeError("%s failed (status %d): %s" % (what, rc, msg))
+
+
+def call(name, *args):
+    """Call an entry point and raise MeshodeError on a non-zero status."""
+    rc = getattr(lib(), name)(*args)
+    check(rc, name)
+    return rc
+
+
+def require_cuda():
+    if not torch.cuda.is_available():
+        raise MeshodeError("meshode_gb300 needs a CUDA device (GB300 / sm_103a); none is available")
+    lib()
+
+
+def ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def stream_ptr(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)

@@ -1,0 +1,651 @@
+// Distance-field build: normalisation, triangle records, Morton codes, stable
+// radix sort, Karras LBVH, bottom-up refit, warp-packet nearest-triangle
+// traversal, and a shared-memory-tiled brute force for small targets.
+// Reference: Mesh::Normalize (src/lib/mesh.cc:66-96) and
+// Mesh::ConstructDistanceField (mesh.cc:106-152), whose
+// igl::point_mesh_squared_distance query (mesh.cc:140) returns the exact
+// squared distance to the nearest triangle; the grid stores its sqrt.
+#include <cfloat>
+
+#include "mo_common.cuh"
+
+namespace mo {
+
+// ---------------------------------------------------------------------------
+// Normalisation
+// ---------------------------------------------------------------------------
+__global__ void k_bbox_init(int* bb) {
+    if (threadIdx.x < 3) bb[threadIdx.x] = INT_MAX;
+    else if (threadIdx.x < 6) bb[threadIdx.x] = INT_MIN;
+}
+
+__global__ void __launch_bounds__(256) k_bbox(const float* __restrict__ V, int64_t n, int* __restrict__ bb) {
+    int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {INT_MIN, INT_MIN, INT_MIN};
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        for (int c = 0; c < 3; ++c) {
+            const float f = V[3 * i + c];
+            if (f != f) continue;  // NaN never wins a comparison in the reference
+            const int k = float_to_ordered(f);
+            lo[c] = min(lo[c], k);
+            hi[c] = max(hi[c], k);
+        }
+    }
+    for (int c = 0; c < 3; ++c) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[c] = min(lo[c], __shfl_xor_sync(0xffffffffu, lo[c], o));
+            hi[c] = max(hi[c], __shfl_xor_sync(0xffffffffu, hi[c], o));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+        for (int c = 0; c < 3; ++c) {
+            atomicMin(&bb[c], lo[c]);
+            atomicMax(&bb[3 + c], hi[c]);
+        }
+    }
+}
+
+// mesh.cc:79-82 in double from the exact float extremes.
+__global__ void k_norm_params(const int* __restrict__ bb, double* __restrict__ prm) {
+    double mn[3], mx[3];
+    for (int c = 0; c < 3; ++c) {
+        mn[c] = (bb[c] == INT_MAX) ? 1e30 : (double)ordered_to_float(bb[c]);
+        mx[c] = (bb[3 + c] == INT_MIN) ? -1e30 : (double)ordered_to_float(bb[3 + c]);
+    }
+    const double e0 = mx[0] - mn[0], e1 = mx[1] - mn[1], e2 = mx[2] - mn[2];
+    const double m12 = (e1 < e2) ? e2 : e1;
+    const double m = (e0 < m12) ? m12 : e0;
+    const double scale = m * 1.1;
+    prm[0] = scale;
+    for (int c = 0; c < 3; ++c) prm[1 + c] = mn[c] - 0.05 * scale;
+}
+
+// normalize.cc:21 / :42, evaluated in double (the reference's FT) once per
+// vertex, rounded to float.
+__global__ void k_normalize(float* __restrict__ V, int64_t n, const double* __restrict__ prm, int inverse) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 3 * n) return;
+    const int c = (int)(i % 3);
+    const double s = prm[0], t = prm[1 + c];
+    const double v = (double)V[i];
+    V[i] = inverse ? (float)__dadd_rn(__dmul_rn(v, s), t) : (float)__ddiv_rn(__dsub_rn(v, t), s);
+}
+
+__global__ void k_normalize_copy(const float* __restrict__ V, int64_t n, const double* __restrict__ prm,
+                                 float* __restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 3 * n) return;
+    const int c = (int)(i % 3);
+    out[i] = (float)__ddiv_rn(__dsub_rn((double)V[i], prm[1 + c]), prm[0]);
+}
+
+// ---------------------------------------------------------------------------
+// Triangle records: 4 float4 = {a, inv|ab|^2}, {b, inv|bc|^2}, {c, inv|ca|^2},
+// {unit normal, nondegenerate flag}.
+// ---------------------------------------------------------------------------
+struct Tri {
+    float4 a, b, c, n;
+};
+
+__device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz) {
+    return ax * bx + ay * by + az * bz;
+}
+
+__device__ Tri make_tri(const float* __restrict__ Vn, int i0, int i1, int i2) {
+    const float ax = Vn[3 * (int64_t)i0], ay = Vn[3 * (int64_t)i0 + 1], az = Vn[3 * (int64_t)i0 + 2];
+    const float bx = Vn[3 * (int64_t)i1], by = Vn[3 * (int64_t)i1 + 1], bz = Vn[3 * (int64_t)i1 + 2];
+    const float cx = Vn[3 * (int64_t)i2], cy = Vn[3 * (int64_t)i2 + 1], cz = Vn[3 * (int64_t)i2 + 2];
+    const float abx = bx - ax, aby = by - ay, abz = bz - az;
+    const float bcx = cx - bx, bcy = cy - by, bcz = cz - bz;
+    const float cax = ax - cx, cay = ay - cy, caz = az - cz;
+    const float lab = dot3(abx, aby, abz, abx, aby, abz);
+    const float lbc = dot3(bcx, bcy, bcz, bcx, bcy, bcz);
+    const float lca = dot3(cax, cay, caz, cax, cay, caz);
+    // normal = ab x ac
+    const float acx = cx - ax, acy = cy - ay, acz = cz - az;
+    float nx = aby * acz - abz * acy, ny = abz * acx - abx * acz, nz = abx * acy - aby * acx;
+    const float nn = dot3(nx, ny, nz, nx, ny, nz);
+    float flag = 0.f;
+    if (nn > 0.f && isfinite(nn)) {
+        const float inv = rsqrtf(nn);
+        nx *= inv; ny *= inv; nz *= inv;
+        flag = 1.f;
+    } else {
+        nx = ny = nz = 0.f;
+    }
+    Tri t;
+    t.a = make_float4(ax, ay, az, lab > 0.f ? 1.0f / lab : 0.f);
+    t.b = make_float4(bx, by, bz, lbc > 0.f ? 1.0f / lbc : 0.f);
+    t.c = make_float4(cx, cy, cz, lca > 0.f ? 1.0f / lca : 0.f);
+    t.n = make_float4(nx, ny, nz, flag);
+    return t;
+}
+
+__device__ __forceinline__ float seg_d2(float px, float py, float pz, float4 a, float ex, float ey, float ez) {
+    const float apx = px - a.x, apy = py - a.y, apz = pz - a.z;
+    float t = dot3(apx, apy, apz, ex, ey, ez) * a.w;
+    t = fminf(fmaxf(t, 0.f), 1.f);
+    const float qx = apx - t * ex, qy = apy - t * ey, qz = apz - t * ez;
+    return dot3(qx, qy, qz, qx, qy, qz);
+}
+
+// Squared distance from p to the triangle: the interior plane distance when
+// the projection falls inside, else the nearest of the three edge segments.
+__device__ __forceinline__ float tri_d2(float px, float py, float pz, const Tri& T) {
+    const float abx = T.b.x - T.a.x, aby = T.b.y - T.a.y, abz = T.b.z - T.a.z;
+    const float bcx = T.c.x - T.b.x, bcy = T.c.y - T.b.y, bcz = T.c.z - T.b.z;
+    const float cax = T.a.x - T.c.x, cay = T.a.y - T.c.y, caz = T.a.z - T.c.z;
+    float d = seg_d2(px, py, pz, T.a, abx, aby, abz);
+    d = fminf(d, seg_d2(px, py, pz, T.b, bcx, bcy, bcz));
+    d = fminf(d, seg_d2(px, py, pz, T.c, cax, cay, caz));
+    if (T.n.w != 0.f) {
+        const float apx = px - T.a.x, apy = py - T.a.y, apz = pz - T.a.z;
+        const float bpx = px - T.b.x, bpy = py - T.b.y, bpz = pz - T.b.z;
+        const float cpx = px - T.c.x, cpy = py - T.c.y, cpz = pz - T.c.z;
+        // (edge x (p - edge start)) . n >= 0 on all three edges <=> inside
+        const float s0 = dot3(aby * apz - abz * apy, abz * apx - abx * apz, abx * apy - aby * apx, T.n.x, T.n.y, T.n.z);
+        const float s1 = dot3(bcy * bpz - bcz * bpy, bcz * bpx - bcx * bpz, bcx * bpy - bcy * bpx, T.n.x, T.n.y, T.n.z);
+        const float s2 = dot3(cay * cpz - caz * cpy, caz * cpx - cax * cpz, cax * cpy - cay * cpx, T.n.x, T.n.y, T.n.z);
+        if (s0 >= 0.f && s1 >= 0.f && s2 >= 0.f) {
+            const float h = dot3(apx, apy, apz, T.n.x, T.n.y, T.n.z);
+            d = fminf(d, h * h);
+        }
+    }
+    return d;
+}
+
+__device__ __forceinline__ Tri load_tri(const float4* __restrict__ tris, int i) {
+    Tri t;
+    t.a = __ldg(tris + 4 * (int64_t)i);
+    t.b = __ldg(tris + 4 * (int64_t)i + 1);
+    t.c = __ldg(tris + 4 * (int64_t)i + 2);
+    t.n = __ldg(tris + 4 * (int64_t)i + 3);
+    return t;
+}
+
+__device__ __forceinline__ void store_tri(float4* __restrict__ tris, int i, const Tri& t) {
+    tris[4 * (int64_t)i] = t.a;
+    tris[4 * (int64_t)i + 1] = t.b;
+    tris[4 * (int64_t)i + 2] = t.c;
+    tris[4 * (int64_t)i + 3] = t.n;
+}
+
+// ---------------------------------------------------------------------------
+// Morton codes (identical float operations to the oracle's restatement).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t spread10(uint32_t x) {
+    x &= 0x3ffu;
+    x = (x | (x << 16)) & 0x030000ffu;
+    x = (x | (x << 8)) & 0x0300f00fu;
+    x = (x | (x << 4)) & 0x030c30c3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+
+__device__ __forceinline__ uint32_t quant10(float c) {
+    float q = MUL(c, 1024.0f);
+    q = fmaxf(q, 0.0f);
+    q = fminf(q, 1023.0f);
+    return (uint32_t)q;
+}
+
+__global__ void k_morton(const float* __restrict__ Vn, const int32_t* __restrict__ F, int64_t nf, int64_t nv,
+                         uint32_t* __restrict__ codes, int* __restrict__ ids, int* __restrict__ status) {
+    const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    const int i0 = F[3 * f], i1 = F[3 * f + 1], i2 = F[3 * f + 2];
+    ids[f] = (int)f;
+    if (i0 < 0 || i1 < 0 || i2 < 0 || i0 >= nv || i1 >= nv || i2 >= nv) {
+        atomicOr(status, 1);
+        codes[f] = 0;
+        return;
+    }
+    float c[3];
+    for (int k = 0; k < 3; ++k) {
+        float s = ADD(Vn[3 * (int64_t)i0 + k], Vn[3 * (int64_t)i1 + k]);
+        s = ADD(s, Vn[3 * (int64_t)i2 + k]);
+        c[k] = __fdiv_rn(s, 3.0f);
+    }
+    codes[f] = (spread10(quant10(c[0])) << 2) | (spread10(quant10(c[1])) << 1) | spread10(quant10(c[2]));
+}
+
+__global__ void k_check_faces(const int32_t* __restrict__ F, int64_t nf, int64_t nv, int* __restrict__ status) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 3 * nf) return;
+    const int v = F[i];
+    if (v < 0 || v >= nv) atomicOr(status, 1);
+}
+
+// Sorted triangle records (leaf order) from the sorted ids.
+__global__ void k_tri_records(const float* __restrict__ Vn, const int32_t* __restrict__ F, int64_t nf,
+                              int64_t nv, const int* __restrict__ order, float4* __restrict__ tris) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nf) return;
+    const int64_t f = order ? order[i] : i;
+    int i0 = F[3 * f], i1 = F[3 * f + 1], i2 = F[3 * f + 2];
+    if (i0 < 0 || i1 < 0 || i2 < 0 || i0 >= nv || i1 >= nv || i2 >= nv) i0 = i1 = i2 = 0;  // flagged earlier
+    store_tri(tris, (int)i, make_tri(Vn, i0, i1, i2));
+}
+
+// ---------------------------------------------------------------------------
+// Karras (2012) binary radix tree over sorted codes.  Node record (64 B):
+//   [0] = (left box lo xyz, left child), [1] = (left box hi xyz, right child),
+//   [2] = (right box lo xyz, -), [3] = (right box hi xyz, -).
+// Children >= 0 are internal nodes, ~i encodes leaf i.  parent[] slots:
+// internal i -> i, leaf j -> (n-1)+j; value = 2*parent + side.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int kdelta(const uint32_t* __restrict__ k, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    const uint32_t a = k[i], b = k[j];
+    if (a != b) return __clz(a ^ b);
+    return 32 + __clz((uint32_t)i ^ (uint32_t)j);
+}
+
+__global__ void k_karras(const uint32_t* __restrict__ k, int n, float4* __restrict__ nodes,
+                         int* __restrict__ parent, int* __restrict__ flags) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    const int d = (kdelta(k, n, i, i + 1) - kdelta(k, n, i, i - 1)) >= 0 ? 1 : -1;
+    const int dmin = kdelta(k, n, i, i - d);
+    int lmax = 2;
+    while (kdelta(k, n, i, i + lmax * d) > dmin) lmax *= 2;
+    int l = 0;
+    for (int t = lmax / 2; t >= 1; t /= 2)
+        if (kdelta(k, n, i, i + (l + t) * d) > dmin) l += t;
+    const int j = i + l * d;
+    const int dnode = kdelta(k, n, i, j);
+    int s = 0, t = l;
+    do {
+        t = (t + 1) / 2;
+        if (kdelta(k, n, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    const int gamma = i + s * d + (d < 0 ? -1 : 0);
+    const int lo = min(i, j), hi = max(i, j);
+    const int left = (lo == gamma) ? ~gamma : gamma;
+    const int right = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+    nodes[4 * (int64_t)i].w = __int_as_float(left);
+    nodes[4 * (int64_t)i + 1].w = __int_as_float(right);
+    parent[left >= 0 ? left : (n - 1) + ~left] = 2 * i;
+    parent[right >= 0 ? right : (n - 1) + ~right] = 2 * i + 1;
+    flags[i] = 0;
+    if (i == 0) parent[0] = -1;
+}
+
+__device__ __forceinline__ void write_child_box(float4* nodes, int p, int side, const float lo[3],
+                                                const float hi[3]) {
+    float* r = reinterpret_cast<float*>(nodes + 4 * (int64_t)p + 2 * side);
+    r[0] = lo[0]; r[1] = lo[1]; r[2] = lo[2];
+    r[4] = hi[0]; r[5] = hi[1]; r[6] = hi[2];
+}
+
+// Bottom-up refit: the second thread to reach a node merges its children.
+__global__ void k_refit(const float4* __restrict__ tris, int n, float4* nodes, const int* __restrict__ parent,
+                        int* flags, float* rootbox, int* status) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const Tri t = load_tri(tris, j);
+    float lo[3] = {fminf(fminf(t.a.x, t.b.x), t.c.x), fminf(fminf(t.a.y, t.b.y), t.c.y),
+                   fminf(fminf(t.a.z, t.b.z), t.c.z)};
+    float hi[3] = {fmaxf(fmaxf(t.a.x, t.b.x), t.c.x), fmaxf(fmaxf(t.a.y, t.b.y), t.c.y),
+                   fmaxf(fmaxf(t.a.z, t.b.z), t.c.z)};
+    int slot = (n - 1) + j;
+    // A Karras tree over distinct (code, index) keys is at most 64 levels
+    // deep; the bound only guards against a corrupted parent array.
+    for (int level = 0;; ++level) {
+        if (level > 128) {
+            atomicOr(status, 4);
+            return;
+        }
+        const int ps = parent[slot];
+        if (ps < 0) break;  // root
+        const int p = ps >> 1, side = ps & 1;
+        write_child_box(nodes, p, side, lo, hi);
+        __threadfence();
+        if (atomicAdd(&flags[p], 1) == 0) return;
+        __threadfence();
+        const float* r = reinterpret_cast<const float*>(nodes + 4 * (int64_t)p);
+        for (int c = 0; c < 3; ++c) {
+            lo[c] = fminf(__ldcg(r + c), __ldcg(r + 8 + c));
+            hi[c] = fmaxf(__ldcg(r + 4 + c), __ldcg(r + 12 + c));
+        }
+        slot = p;
+    }
+    for (int c = 0; c < 3; ++c) {
+        rootbox[c] = lo[c];
+        rootbox[3 + c] = hi[c];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Warp-packet traversal: one warp = a 4x4x2 brick of voxels.  The warp walks
+// the tree together (node and triangle loads are warp-uniform broadcasts);
+// a child is visited when any lane's box distance beats that lane's best.
+// ---------------------------------------------------------------------------
+constexpr int TRAV_WARPS = 4;
+constexpr int TRAV_STACK = 64;
+
+__device__ __forceinline__ float box_d2(float px, float py, float pz, float4 lo, float4 hi) {
+    const float dx = fmaxf(fmaxf(lo.x - px, px - hi.x), 0.f);
+    const float dy = fmaxf(fmaxf(lo.y - py, py - hi.y), 0.f);
+    const float dz = fmaxf(fmaxf(lo.z - pz, pz - hi.z), 0.f);
+    return dx * dx + dy * dy + dz * dz;
+}
+
+__global__ void __launch_bounds__(TRAV_WARPS * 32) k_df_lbvh(const float4* __restrict__ nodes,
+                                                             const float4* __restrict__ tris, int ntri, int N,
+                                                             float* __restrict__ grid, int* __restrict__ status) {
+    __shared__ int stack[TRAV_WARPS][TRAV_STACK];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int bx = (N + 3) / 4, by = (N + 3) / 4, bz = (N + 1) / 2;
+    const int64_t brick = (int64_t)blockIdx.x * TRAV_WARPS + w;
+    if (brick >= (int64_t)bx * by * bz) return;  // warp-uniform
+    const int ix = (int)(brick % bx), iy = (int)((brick / bx) % by), iz = (int)(brick / ((int64_t)bx * by));
+    const int x = ix * 4 + (lane & 3), y = iy * 4 + ((lane >> 2) & 3), z = iz * 2 + (lane >> 4);
+    const bool valid = x < N && y < N && z < N;
+    const float Nf = (float)N;
+    const float px = __fdiv_rn((float)x, Nf), py = __fdiv_rn((float)y, Nf), pz = __fdiv_rn((float)z, Nf);
+    float best = valid ? FLT_MAX : -1.0f;
+    const unsigned FULL = 0xffffffffu;
+    if (ntri == 1) {
+        best = valid ? tri_d2(px, py, pz, load_tri(tris, 0)) : best;
+    } else {
+        int sp = 0;
+        int node = 0;
+        // each node is entered at most once per traversal; the cap only
+        // guards against a corrupted tree
+        const int64_t max_iter = 2 * (int64_t)ntri + 64;
+        for (int64_t iter = 0;; ++iter) {
+            if (iter > max_iter) {
+                if (lane == 0) atomicOr(status, 4);
+                break;
+            }
+            const float4* nd = nodes + 4 * (int64_t)node;
+            const float4 a = __ldg(nd), b = __ldg(nd + 1), c = __ldg(nd + 2), d = __ldg(nd + 3);
+            const int L = __float_as_int(a.w), R = __float_as_int(b.w);
+            const float dl = box_d2(px, py, pz, a, b), dr = box_d2(px, py, pz, c, d);
+            bool wl = __any_sync(FULL, dl < best);
+            bool wr = __any_sync(FULL, dr < best);
+            if (wl && L < 0) {
+                const float t = tri_d2(px, py, pz, load_tri(tris, ~L));
+                if (valid) best = fminf(best, t);
+                wl = false;
+            }
+            if (wr && R < 0) {
+                const float t = tri_d2(px, py, pz, load_tri(tris, ~R));
+                if (valid) best = fminf(best, t);
+                wr = false;
+            }
+            if (wl && wr) {
+                const unsigned nearer_l = __ballot_sync(FULL, valid && dl <= dr);
+                const unsigned act = __ballot_sync(FULL, valid);
+                const bool lfirst = 2 * __popc(nearer_l) >= __popc(act);
+                if (sp >= TRAV_STACK) {  // cannot happen for trees of depth <= 64
+                    if (lane == 0) atomicOr(status, 2);
+                    break;
+                }
+                if (lane == 0) stack[w][sp] = lfirst ? R : L;
+                ++sp;
+                node = lfirst ? L : R;
+            } else if (wl) {
+                node = L;
+            } else if (wr) {
+                node = R;
+            } else {
+                if (sp == 0) break;
+                __syncwarp();
+                node = stack[w][--sp];
+            }
+            __syncwarp();
+        }
+    }
+    if (valid) grid[((int64_t)z * N + y) * N + x] = __fsqrt_rn(best);
+}
+
+// Brute force: each thread one voxel, triangles staged through shared memory.
+constexpr int BF_THREADS = 256, BF_CHUNK = 128;
+
+__global__ void __launch_bounds__(BF_THREADS) k_df_brute(const float4* __restrict__ tris, int ntri, int N,
+                                                         float* __restrict__ grid) {
+    __shared__ float4 sh[BF_CHUNK * 4];
+    const int64_t v = (int64_t)blockIdx.x * BF_THREADS + threadIdx.x;
+    const int64_t nvox = (int64_t)N * N * N;
+    const bool valid = v < nvox;
+    const int x = (int)(v % N), y = (int)((v / N) % N), z = (int)(v / ((int64_t)N * N));
+    const float Nf = (float)N;
+    const float px = __fdiv_rn((float)x, Nf), py = __fdiv_rn((float)y, Nf), pz = __fdiv_rn((float)z, Nf);
+    float best = FLT_MAX;
+    for (int base = 0; base < ntri; base += BF_CHUNK) {
+        const int cnt = min(BF_CHUNK, ntri - base);
+        __syncthreads();
+        for (int k = threadIdx.x; k < cnt * 4; k += BF_THREADS) sh[k] = tris[4 * (int64_t)base + k];
+        __syncthreads();
+        for (int t = 0; t < cnt; ++t) {
+            Tri T;
+            T.a = sh[4 * t]; T.b = sh[4 * t + 1]; T.c = sh[4 * t + 2]; T.n = sh[4 * t + 3];
+            best = fminf(best, tri_d2(px, py, pz, T));
+        }
+    }
+    if (valid) grid[v] = __fsqrt_rn(best);
+}
+
+// ---------------------------------------------------------------------------
+// Scratch layout
+// ---------------------------------------------------------------------------
+struct BuildScratch {
+    float* Vn;
+    float4* tris;
+    uint32_t* codes_a;
+    uint32_t* codes_b;
+    int* ids_a;
+    int* ids_b;
+    float4* nodes;
+    int* parent;
+    int* flags;
+    int* hist;
+    float* rootbox;
+    int* status;
+    size_t bytes;
+};
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static BuildScratch plan_scratch(char* base, int64_t nv, int64_t nf, int method) {
+    BuildScratch s;
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        char* p = base ? base + o : nullptr;
+        o += align256(bytes);
+        return p;
+    };
+    s.status = reinterpret_cast<int*>(take(sizeof(int) * 4));
+    s.rootbox = reinterpret_cast<float*>(take(sizeof(float) * 8));
+    s.Vn = reinterpret_cast<float*>(take(sizeof(float) * 3 * (size_t)nv));
+    s.tris = reinterpret_cast<float4*>(take(sizeof(float4) * 4 * (size_t)nf));
+    if (method == MO_DF_LBVH) {
+        s.codes_a = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * (size_t)nf));
+        s.codes_b = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * (size_t)nf));
+        s.ids_a = reinterpret_cast<int*>(take(sizeof(int) * (size_t)nf));
+        s.ids_b = reinterpret_cast<int*>(take(sizeof(int) * (size_t)nf));
+        s.nodes = reinterpret_cast<float4*>(take(sizeof(float4) * 4 * (size_t)(nf > 1 ? nf - 1 : 1)));
+        s.parent = reinterpret_cast<int*>(take(sizeof(int) * (size_t)(2 * nf)));
+        s.flags = reinterpret_cast<int*>(take(sizeof(int) * (size_t)nf));
+        s.hist = reinterpret_cast<int*>(take(sizeof(int) * radix_hist_ints((int)nf)));
+    } else {
+        s.codes_a = s.codes_b = nullptr;
+        s.ids_a = s.ids_b = nullptr;
+        s.nodes = nullptr;
+        s.parent = s.flags = s.hist = nullptr;
+    }
+    s.bytes = o;
+    return s;
+}
+
+}  // namespace mo
+
+using namespace mo;
+
+extern "C" int mo_bbox(const float* V, int64_t n, int32_t* bbox6, void* stream) {
+    MO_CHECK_ARG(n >= 0, "negative vertex count");
+    MO_CHECK_ARG(bbox6 && (n == 0 || V), "null pointer");
+    cudaStream_t s = as_stream(stream);
+    k_bbox_init<<<1, 32, 0, s>>>(bbox6);
+    if (n > 0) {
+        const int blocks = std::min(ceil_div(n, 256), 4 * device_sm_count());
+        k_bbox<<<blocks, 256, 0, s>>>(V, n, bbox6);
+    }
+    MO_LAUNCH_CHECK("k_bbox");
+    return MO_OK;
+}
+
+extern "C" int mo_norm_params(const int32_t* bbox6, double* params4, void* stream) {
+    MO_CHECK_ARG(bbox6 && params4, "null pointer");
+    k_norm_params<<<1, 1, 0, as_stream(stream)>>>(bbox6, params4);
+    MO_LAUNCH_CHECK("k_norm_params");
+    return MO_OK;
+}
+
+extern "C" int mo_normalize(float* V, int64_t n, const double* params4, int inverse, void* stream) {
+    MO_CHECK_ARG(n >= 0, "negative vertex count");
+    if (n == 0) return MO_OK;
+    MO_CHECK_ARG(V && params4, "null pointer");
+    k_normalize<<<ceil_div(3 * n, 256), 256, 0, as_stream(stream)>>>(V, n, params4, inverse);
+    MO_LAUNCH_CHECK("k_normalize");
+    return MO_OK;
+}
+
+extern "C" int mo_df_method_for(int64_t nf, int N) {
+    // Brute force tests every voxel against every triangle; below ~3e8 pair
+    // tests it beats building and walking the tree.
+    const double pairs = (double)nf * (double)N * N * N;
+    return (nf <= 64 || pairs <= 3.0e8) ? MO_DF_BRUTE : MO_DF_LBVH;
+}
+
+extern "C" size_t mo_df_build_scratch_bytes(int64_t nv, int64_t nf, int N, int method) {
+    if (nv < 0 || nf < 0) return 0;
+    if (method == MO_DF_AUTO) method = mo_df_method_for(nf, N);
+    return plan_scratch(nullptr, nv, nf, method).bytes;
+}
+
+extern "C" int mo_df_build(const float* V, int64_t nv, const int32_t* F, int64_t nf, int N, const double* params4,
+                           int method, void* scratch, size_t scratch_bytes, float* grid_out, int32_t* status_out,
+                           void* stream) {
+    MO_CHECK_ARG(nv > 0 && nf > 0, "target mesh must have vertices and faces (nv=%lld nf=%lld)", (long long)nv,
+                 (long long)nf);
+    MO_CHECK_ARG(nf < ((int64_t)1 << 30) && nv < ((int64_t)1 << 31), "target mesh too large");
+    MO_CHECK_ARG(N >= 2 && N <= 2048, "grid resolution out of range (%d)", N);
+    MO_CHECK_ARG(V && F && params4 && grid_out, "null pointer");
+    MO_CHECK_ARG(method == MO_DF_AUTO || method == MO_DF_BRUTE || method == MO_DF_LBVH, "unknown method %d", method);
+    if (method == MO_DF_AUTO) method = mo_df_method_for(nf, N);
+    cudaStream_t s = as_stream(stream);
+    const size_t need = plan_scratch(nullptr, nv, nf, method).bytes;
+    void* owned = nullptr;
+    if (!scratch) {
+        MO_CUDA(cudaMallocAsync(&owned, need, s));
+        scratch = owned;
+    } else if (scratch_bytes < need) {
+        set_error("DF build scratch too small: %zu < %zu", scratch_bytes, need);
+        return MO_ERR_SCRATCH;
+    }
+    BuildScratch S = plan_scratch(reinterpret_cast<char*>(scratch), nv, nf, method);
+    int rc = MO_OK;
+    auto fail = [&](cudaError_t e, const char* where) {
+        rc = cuda_status(e, where);
+    };
+    int* st = status_out ? reinterpret_cast<int*>(status_out) : S.status;
+    do {
+        cudaError_t e = cudaSuccess;
+        if (!status_out) {
+            e = cudaMemsetAsync(S.status, 0, sizeof(int) * 4, s);
+            if (e != cudaSuccess) { fail(e, "memset"); break; }
+        }
+        k_normalize_copy<<<ceil_div(3 * nv, 256), 256, 0, s>>>(V, nv, params4, S.Vn);
+        if (method == MO_DF_BRUTE) {
+            k_check_faces<<<ceil_div(nf, 256), 256, 0, s>>>(F, nf, nv, st);
+            k_tri_records<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, nullptr, S.tris);
+            const int64_t nvox = (int64_t)N * N * N;
+            k_df_brute<<<ceil_div(nvox, BF_THREADS), BF_THREADS, 0, s>>>(S.tris, (int)nf, N, grid_out);
+        } else {
+            k_morton<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.codes_a, S.ids_a, st);
+            e = radix_sort_pairs(S.codes_a, S.ids_a, S.codes_b, S.ids_b, (int)nf, 30, S.hist, s);
+            if (e != cudaSuccess) { fail(e, "radix_sort_pairs"); break; }
+            k_tri_records<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.ids_a, S.tris);
+            if (nf > 1) {
+                k_karras<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.codes_a, (int)nf, S.nodes, S.parent, S.flags);
+                k_refit<<<ceil_div(nf, 256), 256, 0, s>>>(S.tris, (int)nf, S.nodes, S.parent, S.flags, S.rootbox, st);
+            }
+            const int64_t bricks = (int64_t)((N + 3) / 4) * ((N + 3) / 4) * ((N + 1) / 2);
+            k_df_lbvh<<<ceil_div(bricks, TRAV_WARPS), TRAV_WARPS * 32, 0, s>>>(S.nodes, S.tris, (int)nf, N,
+                                                                               grid_out, st);
+        }
+        e = cudaGetLastError();
+        if (e != cudaSuccess) { fail(e, "df build kernels"); break; }
+    } while (0);
+    if (rc == MO_OK && !status_out) {
+        int status = 0;
+        cudaError_t e = cudaMemcpyAsync(&status, S.status, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = cuda_status(e, "df build status");
+        else if (status & 1) { set_error("face index out of range [0, %lld)", (long long)nv); rc = MO_ERR_DEVICE; }
+        else if (status & 2) { set_error("LBVH traversal stack overflow"); rc = MO_ERR_DEVICE; }
+        else if (status & 4) { set_error("LBVH is malformed (refit or traversal bound exceeded)"); rc = MO_ERR_DEVICE; }
+    }
+    if (owned) cudaFreeAsync(owned, s);
+    return rc;
+}
+
+extern "C" int mo_lbvh_build(const float* V, int64_t nv, const int32_t* F, int64_t nf, const double* params4,
+                             void* scratch, size_t scratch_bytes, uint32_t* sorted_codes, int32_t* order,
+                             int32_t* left, int32_t* right, float* root_box, void* stream) {
+    MO_CHECK_ARG(nv > 0 && nf > 0, "empty mesh");
+    MO_CHECK_ARG(nf < ((int64_t)1 << 30) && nv < ((int64_t)1 << 31), "mesh too large");
+    MO_CHECK_ARG(V && F && params4 && sorted_codes && order, "null pointer");
+    MO_CHECK_ARG(nf == 1 || (left && right), "null child arrays");
+    cudaStream_t s = as_stream(stream);
+    const size_t need = plan_scratch(nullptr, nv, nf, MO_DF_LBVH).bytes;
+    void* owned = nullptr;
+    if (!scratch) {
+        MO_CUDA(cudaMallocAsync(&owned, need, s));
+        scratch = owned;
+    } else if (scratch_bytes < need) {
+        set_error("LBVH scratch too small: %zu < %zu", scratch_bytes, need);
+        return MO_ERR_SCRATCH;
+    }
+    BuildScratch S = plan_scratch(reinterpret_cast<char*>(scratch), nv, nf, MO_DF_LBVH);
+    int rc = MO_OK;
+    cudaError_t e = cudaMemsetAsync(S.status, 0, sizeof(int) * 4, s);
+    if (e == cudaSuccess) {
+        k_normalize_copy<<<ceil_div(3 * nv, 256), 256, 0, s>>>(V, nv, params4, S.Vn);
+        k_morton<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.codes_a, S.ids_a, S.status);
+        e = radix_sort_pairs(S.codes_a, S.ids_a, S.codes_b, S.ids_b, (int)nf, 30, S.hist, s);
+    }
+    if (e == cudaSuccess) {
+        k_tri_records<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.ids_a, S.tris);
+        if (nf > 1) {
+            k_karras<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.codes_a, (int)nf, S.nodes, S.parent, S.flags);
+            k_refit<<<ceil_div(nf, 256), 256, 0, s>>>(S.tris, (int)nf, S.nodes, S.parent, S.flags, S.rootbox,
+                                                      S.status);
+        }
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(sorted_codes, S.codes_a, 4 * nf, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(order, S.ids_a, 4 * nf, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess && nf > 1) {
+        // child indices live in the .w lanes of node words 0 and 1
+        e = cudaMemcpy2DAsync(left, sizeof(int32_t), reinterpret_cast<const char*>(S.nodes) + 12, 64, sizeof(int32_t),
+                              (size_t)(nf - 1), cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpy2DAsync(right, sizeof(int32_t), reinterpret_cast<const char*>(S.nodes) + 28, 64,
+                                  sizeof(int32_t), (size_t)(nf - 1), cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess && root_box)
+            e = cudaMemcpyAsync(root_box, S.rootbox, 6 * sizeof(float), cudaMemcpyDeviceToDevice, s);
+    }
+    if (e != cudaSuccess) rc = cuda_status(e, "mo_lbvh_build");
+    if (rc == MO_OK) {
+        int status = 0;
+        e = cudaMemcpyAsync(&status, S.status, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = cuda_status(e, "mo_lbvh_build status");
+        else if (status & 1) { set_error("face index out of range [0, %lld)", (long long)nv); rc = MO_ERR_DEVICE; }
+    }
+    if (owned) cudaFreeAsync(owned, s);
+    return rc;
+}

@@ -1,0 +1,381 @@
+"""CPU oracle with the reference's ``pyDeform`` interface (test infrastructure).
+
+This module is the checker for ``meshode_gb300.pyDeform``: it restates the
+reference's pybind11 module (src/interface/pydeform.cc:14-39) on CPU float32
+tensors, calling the C restatement in ``meshode_oracle.c`` through ctypes.
+Only tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py``
+import it.
+
+Parity status: UNPINNED against the reference (the reference cannot be built
+here and ships no golden vectors); see the header of meshode_oracle.c.
+"""
+import ctypes
+import os
+
+import numpy as np
+import torch
+
+from . import build as _build
+
+_lib = None
+
+
+def lib():
+    """Load (building if needed) the oracle shared library."""
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = ctypes.CDLL(path)
+        P = ctypes.c_void_p
+        i64 = ctypes.c_int64
+        L.orc_distance_float.restype = ctypes.c_float
+        L.orc_distance_float.argtypes = [P, ctypes.c_int, P]
+        L.orc_distance_jet.argtypes = [P, ctypes.c_int, P, P]
+        L.orc_dfloss_forward.argtypes = [P, i64, P, ctypes.c_int, P]
+        L.orc_dfloss_backward.argtypes = [P, i64, P, ctypes.c_int, P]
+        L.orc_edge_offsets.argtypes = [P, P, i64, ctypes.c_int, P]
+        L.orc_edge_forward.argtypes = [P, P, i64, ctypes.c_int, P, P]
+        L.orc_edge_backward.argtypes = [P, i64, P, i64, ctypes.c_int, P, P]
+        L.orc_normalize_params.argtypes = [P, i64, P, P]
+        L.orc_normalize_double.argtypes = [P, i64, ctypes.c_double, P, P]
+        L.orc_normalize_by_template.argtypes = [P, i64, ctypes.c_double, P]
+        L.orc_denormalize_by_template.argtypes = [P, i64, ctypes.c_double, P]
+        L.orc_point_tri_dist2.restype = ctypes.c_double
+        L.orc_point_tri_dist2.argtypes = [P, P, P, P]
+        L.orc_df_bruteforce.argtypes = [P, P, i64, ctypes.c_int, P, i64, P]
+        L.orc_df_bvh.restype = ctypes.c_int
+        L.orc_df_bvh.argtypes = [P, P, i64, ctypes.c_int, P, i64, P, ctypes.c_int]
+        L.orc_morton_codes.argtypes = [P, P, i64, P]
+        L.orc_sort_codes.argtypes = [P, i64, P, P]
+        L.orc_karras.argtypes = [P, ctypes.c_int, P, P]
+        L.orc_trunc_i32.restype = ctypes.c_int
+        L.orc_trunc_i32.argtypes = [ctypes.c_float]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def _f32(t):
+    a = t.detach().cpu().numpy() if isinstance(t, torch.Tensor) else np.asarray(t)
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _i32(t):
+    a = t.detach().cpu().numpy() if isinstance(t, torch.Tensor) else np.asarray(t)
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+# --------------------------------------------------------------------------
+# Raw numpy-level helpers
+# --------------------------------------------------------------------------
+def normalize_params(V):
+    """Mesh::Normalize (src/lib/mesh.cc:66-96): (scale, trans[3]) in double."""
+    V = _f32(V)
+    scale = np.zeros(1, np.float64)
+    trans = np.zeros(3, np.float64)
+    lib().orc_normalize_params(_p(V), V.shape[0], _p(scale), _p(trans))
+    return float(scale[0]), trans
+
+
+def normalized_double(V, scale, trans):
+    """Normalised target vertices in double (mesh.cc:83-85)."""
+    V = _f32(V)
+    out = np.empty(V.shape, np.float64)
+    tr = np.ascontiguousarray(trans, np.float64)
+    lib().orc_normalize_double(_p(V), V.shape[0], scale, _p(tr), _p(out))
+    return out
+
+
+def df_build(Vn64, F, N, voxels=None, method="bvh", threads=0):
+    """Unsigned DF of a normalised target (mesh.cc:106-152) in FP64.
+
+    Returns sqrt(min squared distance) for every voxel (flattened [z][y][x])
+    or for the given voxel indices.
+    """
+    Vn64 = np.ascontiguousarray(Vn64, np.float64)
+    F = _i32(F)
+    if voxels is None:
+        nvox = N ** 3
+        vox = None
+    else:
+        vox = np.ascontiguousarray(voxels, np.int64)
+        nvox = vox.shape[0]
+    out = np.empty(nvox, np.float64)
+    if method == "brute":
+        lib().orc_df_bruteforce(_p(Vn64), _p(F), F.shape[0], N, _p(vox), nvox, _p(out))
+    else:
+        rc = lib().orc_df_bvh(_p(Vn64), _p(F), F.shape[0], N, _p(vox), nvox, _p(out), threads)
+        if rc != 0:
+            raise RuntimeError("orc_df_bvh failed: %d" % rc)
+    return out
+
+
+def distance_float(grid, N, p):
+    g = np.ascontiguousarray(grid, np.float32)
+    pp = np.ascontiguousarray(p, np.float32)
+    return lib().orc_distance_float(_p(g), N, _p(pp))
+
+
+def distance_jet(grid, N, p):
+    g = np.ascontiguousarray(grid, np.float32)
+    pp = np.ascontiguousarray(p, np.float32)
+    out = np.zeros(4, np.float32)
+    lib().orc_distance_jet(_p(g), N, _p(pp), _p(out))
+    return out
+
+
+def dfloss_forward(V, grid, N):
+    V = _f32(V); g = np.ascontiguousarray(grid, np.float32)
+    L = np.empty(V.shape[0], np.float32)
+    lib().orc_dfloss_forward(_p(V), V.shape[0], _p(g), N, _p(L))
+    return L
+
+
+def dfloss_backward(V, grid, N):
+    V = _f32(V); g = np.ascontiguousarray(grid, np.float32)
+    Gd = np.empty((V.shape[0], 3), np.float32)
+    lib().orc_dfloss_backward(_p(V), V.shape[0], _p(g), N, _p(Gd))
+    return Gd
+
+
+def edge_count(idx, kind):
+    return idx.shape[0] * 3 if kind == 0 else idx.shape[0]
+
+
+def edge_offsets(V, idx, kind):
+    V = _f32(V); idx = _i32(idx)
+    nh = edge_count(idx, kind)
+    off = np.empty((nh, 3), np.float32)
+    lib().orc_edge_offsets(_p(V), _p(idx), nh, kind, _p(off))
+    return off
+
+
+def edge_forward(V, idx, kind, off):
+    V = _f32(V); idx = _i32(idx); off = _f32(off)
+    nh = edge_count(idx, kind)
+    L = np.empty((nh, 3), np.float32)
+    lib().orc_edge_forward(_p(V), _p(idx), nh, kind, _p(off), _p(L))
+    return L
+
+
+def edge_backward(V, idx, kind, off):
+    V = _f32(V); idx = _i32(idx); off = _f32(off)
+    nh = edge_count(idx, kind)
+    Gd = np.empty((V.shape[0], 3), np.float32)
+    lib().orc_edge_backward(_p(V), V.shape[0], _p(idx), nh, kind, _p(off), _p(Gd))
+    return Gd
+
+
+def morton_codes(Vn32, F):
+    Vn32 = _f32(Vn32); F = _i32(F)
+    codes = np.empty(F.shape[0], np.uint32)
+    lib().orc_morton_codes(_p(Vn32), _p(F), F.shape[0], _p(codes))
+    return codes
+
+
+def sort_codes(codes):
+    codes = np.ascontiguousarray(codes, np.uint32)
+    sc = np.empty_like(codes)
+    perm = np.empty(codes.shape[0], np.int32)
+    lib().orc_sort_codes(_p(codes), codes.shape[0], _p(sc), _p(perm))
+    return sc, perm
+
+
+def karras(sorted_codes):
+    k = np.ascontiguousarray(sorted_codes, np.uint32)
+    n = k.shape[0]
+    left = np.zeros(max(n - 1, 0), np.int32)
+    right = np.zeros(max(n - 1, 0), np.int32)
+    if n > 1:
+        lib().orc_karras(_p(k), n, _p(left), _p(right))
+    return left, right
+
+
+# --------------------------------------------------------------------------
+# OBJ I/O with the reference's quirks (src/lib/mesh.cc:14-64)
+# --------------------------------------------------------------------------
+def read_obj(path):
+    """Mesh::ReadOBJ: 'v x y z' parsed as double, 'f a b c' keeps the leading
+    digits of each token (a/b/c -> a), 1-based; reading stops at the first line
+    of 256 or more characters (std::istream::getline with a 256-byte buffer)."""
+    V, F = [], []
+    with open(path, "rb") as fh:
+        for raw in fh:
+            line = raw.rstrip(b"\n")
+            if len(line) >= 256:
+                break
+            toks = line.split()
+            if not toks:
+                continue
+            if toks[0] == b"v":
+                V.append([float(t) for t in toks[1:4]])
+            elif toks[0] == b"f":
+                f = []
+                for t in toks[1:4]:
+                    i = 0
+                    for ch in t:
+                        if ch == ord("/"):
+                            break
+                        i = i * 10 + (ch - 48)
+                    f.append(i - 1)
+                F.append(f)
+    return np.asarray(V, np.float64).reshape(-1, 3), np.asarray(F, np.int64).reshape(-1, 3)
+
+
+def write_obj(path, V, F):
+    """Mesh::WriteOBJ (mesh.cc:46-64): default ostream precision (%g)."""
+    V = np.asarray(V, np.float64)
+    F = np.asarray(F, np.int64)
+    with open(path, "w") as fh:
+        for v in V:
+            fh.write("v %g %g %g\n" % (v[0], v[1], v[2]))
+        for f in F:
+            fh.write("f %d %d %d\n" % (f[0] + 1, f[1] + 1, f[2] + 1))
+
+
+# --------------------------------------------------------------------------
+# pyDeform-compatible module surface (src/interface/pydeform.cc:14-39)
+# --------------------------------------------------------------------------
+class _Params:
+    def __init__(self):
+        self.scale = 1.0
+        self.trans = np.zeros(3)
+        self.N = 0
+        self.grid = None          # float32 [N^3], [z][y][x]
+        self.Vn64 = None
+        self.F = None
+        self.edge_offset = None   # float32 [H,3]
+
+
+_params = []
+
+
+def GetParams(pid):
+    return _params[pid]
+
+
+def LoadMesh(path):
+    """mesh_tensor.cc:87-100: raw (un-normalised) float32 V and int32 F."""
+    V, F = read_obj(path)
+    return [torch.from_numpy(V.astype(np.float32)), torch.from_numpy(F.astype(np.int32))]
+
+
+def SaveMesh(path, V, F):
+    write_obj(path, _f32(V).astype(np.float64), _i32(F))
+
+
+def InitializeDeformTemplate(V, F, symmetry, N, df_method="bvh", grid=None):
+    """deform_params.cc:16-40.  ``symmetry`` is accepted and, as in the
+    reference, has no effect (it is applied to an empty mesh)."""
+    p = _Params()
+    p.scale, p.trans = normalize_params(V)
+    p.N = int(N)
+    p.F = _i32(F)
+    p.Vn64 = normalized_double(V, p.scale, p.trans)
+    if grid is not None:
+        p.grid = np.ascontiguousarray(grid, np.float32).reshape(-1)
+    else:
+        p.grid = df_build(p.Vn64, p.F, p.N, method=df_method).astype(np.float32)
+    _params.append(p)
+    return len(_params) - 1
+
+
+def NormalizeByTemplate(V, pid):
+    p = _params[pid]
+    a = V.detach().numpy() if isinstance(V, torch.Tensor) else V
+    assert a.dtype == np.float32 and a.flags.c_contiguous
+    lib().orc_normalize_by_template(_p(a), a.shape[0], p.scale, _p(np.ascontiguousarray(p.trans)))
+
+
+def DenormalizeByTemplate(V, pid):
+    p = _params[pid]
+    a = V.detach().numpy() if isinstance(V, torch.Tensor) else V
+    assert a.dtype == np.float32 and a.flags.c_contiguous
+    lib().orc_denormalize_by_template(_p(a), a.shape[0], p.scale, _p(np.ascontiguousarray(p.trans)))
+
+
+def StoreRigidityInformation(V, F, pid):
+    _params[pid].edge_offset = edge_offsets(V, F, 0)
+
+
+def StoreGraphInformation(V, E, pid):
+    _params[pid].edge_offset = edge_offsets(V, E, 1)
+
+
+def DistanceFieldLoss_forward(V, pid):
+    p = _params[pid]
+    return torch.from_numpy(dfloss_forward(V, p.grid, p.N))
+
+
+def DistanceFieldLoss_backward(V, pid):
+    p = _params[pid]
+    return torch.from_numpy(dfloss_backward(V, p.grid, p.N))
+
+
+def RigidEdgeLoss_forward(V, F, pid):
+    return torch.from_numpy(edge_forward(V, F, 0, _params[pid].edge_offset))
+
+
+def RigidEdgeLoss_backward(V, F, pid):
+    return torch.from_numpy(edge_backward(V, F, 0, _params[pid].edge_offset))
+
+
+def GraphEdgeLoss_forward(V, E, pid):
+    return torch.from_numpy(edge_forward(V, E, 1, _params[pid].edge_offset))
+
+
+def GraphEdgeLoss_backward(V, E, pid):
+    return torch.from_numpy(edge_backward(V, E, 1, _params[pid].edge_offset))
+
+
+# --------------------------------------------------------------------------
+# The plain CPU optimiser loop (src/python/rigid_deform.py:28-41 with
+# RigidLossFunction from src/python/layers/rigid_loss_layer.py:7-27).
+# --------------------------------------------------------------------------
+def rigid_loss(V, F, pid):
+    """RigidLossFunction.forward: 0.5*sum(d^2) + 0.5*sum(r^2)."""
+    lossD = DistanceFieldLoss_forward(V, pid) * 0.5
+    lossR = RigidEdgeLoss_forward(V, F, pid) * 0.5
+    return lossD.sum() + lossR.sum()
+
+
+def rigid_grad(V, F, pid, grad_h=1.0):
+    """RigidLossFunction.backward: grad_h*(gD + gR)."""
+    gD = DistanceFieldLoss_backward(V, pid)
+    gR = RigidEdgeLoss_backward(V, F, pid)
+    return grad_h * (gD + gR)
+
+
+def graph_loss_grad(V, E, pid, rigidity2):
+    """GraphLossFunction (src/python/layers/graph_loss_layer.py:9-43):
+    loss = 0.5*sum(d^2) + rigidity2*0.5*sum(r^2); DF gradient masked where
+    0.5*d^2 >= 0.5*0.03*0.03."""
+    lossD = DistanceFieldLoss_forward(V, pid) * 0.5
+    lossR = GraphEdgeLoss_forward(V, E, pid) * 0.5
+    mask = (lossD < (0.5 * 0.03 * 0.03)).view(-1, 1).expand(-1, 3)
+    loss = lossD.sum() + lossR.sum() * float(torch.tensor(rigidity2).item())
+    gD = DistanceFieldLoss_backward(V, pid)
+    gR = GraphEdgeLoss_backward(V, E, pid)
+    gD = gD * mask
+    r2 = float(torch.tensor(rigidity2, dtype=torch.float32).item())
+    return loss, gD + gR * r2
+
+
+def rigid_fit(src_V, src_F, pid, steps, lr=1e-3, loss_every=0, threads=None):
+    """Adam loop of rigid_deform.py:32-41 on CPU, returns (V, losses)."""
+    if threads is not None:
+        torch.set_num_threads(threads)
+    V = torch.nn.Parameter(src_V.clone())
+    opt = torch.optim.Adam([V], lr=lr)
+    losses = []
+    for it in range(steps):
+        opt.zero_grad()
+        with torch.no_grad():
+            if loss_every and it % loss_every == 0:
+                losses.append(float(rigid_loss(V.data, src_F, pid)))
+            V.grad = rigid_grad(V.data, src_F, pid)
+        opt.step()
+    return V.detach(), losses

@@ -1,0 +1,68 @@
+"""The C-ABI library loads and exports every function include/meshode.h
+declares (no compute: this runs without a GPU)."""
+import ctypes
+import os
+import re
+
+from meshode_gb300 import _lib as L
+from meshode_gb300 import build as B
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "meshode.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\*?\s*(mo_[A-Za-z0-9_]+)\s*\(", src, flags=re.M)
+    return sorted(set(names))
+
+
+def test_library_builds_and_exports_header_symbols():
+    B.build()
+    lib = ctypes.CDLL(L.LIB_PATH)
+    names = declared_functions()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_binding_covers_header():
+    assert set(declared_functions()) == set(L.exported_symbols())
+
+
+def test_struct_layout_matches_library():
+    B.build()
+    a, b = ctypes.c_size_t(), ctypes.c_size_t()
+    L.call("mo_abi_sizes", ctypes.byref(a), ctypes.byref(b))
+    assert a.value == ctypes.sizeof(L.MoPair)
+    assert b.value == ctypes.sizeof(L.MoTile)
+
+
+def test_host_side_queries_without_gpu():
+    B.build()
+    lib = L.lib()
+    assert lib.mo_version() >= 100
+    assert lib.mo_grid_bytes(64, L.MO_LAYOUT_LINEAR) == 64 ** 3 * 4
+    assert lib.mo_grid_bytes(64, L.MO_LAYOUT_CELL) == 63 ** 3 * 32
+    assert lib.mo_grid_bytes(64, 7) == 0
+    assert lib.mo_edge_count(10, L.MO_EDGES_FACES) == 30
+    assert lib.mo_edge_count(10, L.MO_EDGES_LIST) == 10
+    assert lib.mo_edge_count(10, 5) == -1
+    assert lib.mo_df_method_for(20, 64) == L.MO_DF_BRUTE
+    assert lib.mo_df_method_for(1_310_720, 256) == L.MO_DF_LBVH
+    assert lib.mo_df_build_scratch_bytes(1000, 2000, 64, L.MO_DF_LBVH) > 2000 * 64
+    assert lib.mo_edge_csr_bytes(100, 50, L.MO_EDGES_FACES) >= 4 * (101 + 4 * 150)
+
+
+def test_argument_errors_are_reported_without_gpu():
+    B.build()
+    lib = L.lib()
+    rc = lib.mo_dfloss_forward(None, 10, None, 64, L.MO_LAYOUT_LINEAR, None, None)
+    assert rc == L.MO_ERR_INVALID
+    assert b"null" in lib.mo_last_error()
+    rc = lib.mo_dfloss_backward(None, 10, None, 1, L.MO_LAYOUT_LINEAR, None, None)
+    assert rc == L.MO_ERR_INVALID and b"resolution" in lib.mo_last_error()
+    rc = lib.mo_df_build(None, 0, None, 0, 64, None, 0, None, 0, None, None, None)
+    assert rc == L.MO_ERR_INVALID
+    rc = lib.mo_edge_offsets(None, 10, None, 5, 9, None, None)
+    assert rc == L.MO_ERR_INVALID and b"kind" in lib.mo_last_error()

@@ -1,0 +1,111 @@
+"""Rigid / graph edge losses on the GPU against the oracle's serial loops.
+
+Reference: src/interface/rigid_layer.cc:11-133 and graph_layer.cc:11-135.  The
+backward pass is a per-vertex reduction over a CSR sorted in half-edge order,
+so it must reproduce the reference's serial scatter bit for bit.
+"""
+import numpy as np
+import pytest
+import torch
+
+from meshode_gb300 import meshgen
+from meshode_gb300 import pyDeform as PD
+
+pytestmark = pytest.mark.gpu
+
+
+def _template(cuda, N=16):
+    V, F = meshgen.icosphere(1)
+    return PD.InitializeDeformTemplate(torch.from_numpy(V.astype(np.float32)), torch.from_numpy(F.astype(np.int32)),
+                                       0, N)
+
+
+def _same(a, b):
+    a = np.asarray(a, np.float32)
+    b = np.asarray(b, np.float32)
+    eq = (a == b) | (np.isnan(a) & np.isnan(b))
+    return bool(eq.all()), int((~eq).sum())
+
+
+@pytest.mark.parametrize("level", [1, 3])
+def test_rigid_edges_bitexact(cuda, orc, level):
+    rng = np.random.Generator(np.random.PCG64(level))
+    V, F = meshgen.icosphere(level)
+    V0 = (V * 0.3 + 0.5).astype(np.float32)
+    F = F.astype(np.int32)
+    pid = _template(cuda)
+    Vt = torch.from_numpy(V0)
+    Ft = torch.from_numpy(F)
+    PD.StoreRigidityInformation(Vt, Ft, pid)
+    off = orc.edge_offsets(V0, F, 0)
+    ok, _ = _same(PD.GetParams(pid).edge.offsets.cpu().numpy(), off)
+    assert ok
+    V1 = (V0 + rng.normal(scale=0.01, size=V0.shape)).astype(np.float32)
+    for dev in ("cpu", cuda):
+        Vx = torch.from_numpy(V1).to(dev)
+        Fx = Ft.to(dev)
+        f = PD.RigidEdgeLoss_forward(Vx, Fx, pid).cpu().numpy()
+        b = PD.RigidEdgeLoss_backward(Vx, Fx, pid).cpu().numpy()
+        ok, n = _same(f, orc.edge_forward(V1, F, 0, off))
+        assert ok, n
+        ok, n = _same(b, orc.edge_backward(V1, F, 0, off))
+        assert ok, n
+
+
+def test_graph_edges_degenerate_and_duplicates(cuda, orc):
+    rng = np.random.Generator(np.random.PCG64(7))
+    nv = 500
+    V0 = rng.uniform(0, 1, size=(nv, 3)).astype(np.float32)
+    E = rng.integers(0, nv, size=(3000, 2)).astype(np.int32)
+    E[:50, 1] = E[:50, 0]          # degenerate v0 == v1
+    E[50:100] = E[100:150]         # duplicates
+    E[150:200] = E[200:250][:, ::-1]  # reversed duplicates
+    E = np.ascontiguousarray(E)
+    pid = _template(cuda)
+    PD.StoreGraphInformation(torch.from_numpy(V0), torch.from_numpy(E), pid)
+    off = orc.edge_offsets(V0, E, 1)
+    V1 = (V0 + rng.normal(scale=0.05, size=V0.shape)).astype(np.float32)
+    Vx = torch.from_numpy(V1).to(cuda)
+    Ex = torch.from_numpy(E).to(cuda)
+    ok, n = _same(PD.GraphEdgeLoss_forward(Vx, Ex, pid).cpu().numpy(), orc.edge_forward(V1, E, 1, off))
+    assert ok, n
+    ok, n = _same(PD.GraphEdgeLoss_backward(Vx, Ex, pid).cpu().numpy(), orc.edge_backward(V1, E, 1, off))
+    assert ok, n
+
+
+def test_isolated_vertices_and_high_degree(cuda, orc):
+    # a fan: vertex 0 connected to 2000 others (a long CSR row), plus isolated vertices
+    nv = 2100
+    rng = np.random.Generator(np.random.PCG64(9))
+    V0 = rng.uniform(0, 1, size=(nv, 3)).astype(np.float32)
+    F = np.stack([np.zeros(1999), np.arange(1, 2000), np.arange(2, 2001)], 1).astype(np.int32)
+    pid = _template(cuda)
+    PD.StoreRigidityInformation(torch.from_numpy(V0), torch.from_numpy(F), pid)
+    off = orc.edge_offsets(V0, F, 0)
+    V1 = (V0 + rng.normal(scale=0.02, size=V0.shape)).astype(np.float32)
+    b = PD.RigidEdgeLoss_backward(torch.from_numpy(V1).to(cuda), torch.from_numpy(F).to(cuda), pid).cpu().numpy()
+    ok, n = _same(b, orc.edge_backward(V1, F, 0, off))
+    assert ok, n
+    assert np.all(b[2001:] == 0)
+
+
+def test_bad_index_raises(cuda):
+    V0 = np.zeros((10, 3), np.float32)
+    F = np.array([[0, 1, 2], [3, 4, 10]], np.int32)
+    pid = _template(cuda)
+    with pytest.raises(RuntimeError):
+        PD.StoreRigidityInformation(torch.from_numpy(V0), torch.from_numpy(F), pid)
+    F2 = np.array([[0, 1, -1]], np.int32)
+    with pytest.raises(RuntimeError):
+        PD.StoreRigidityInformation(torch.from_numpy(V0), torch.from_numpy(F2), pid)
+
+
+def test_empty_edges(cuda):
+    V0 = np.zeros((4, 3), np.float32)
+    F = np.zeros((0, 3), np.int32)
+    pid = _template(cuda)
+    PD.StoreRigidityInformation(torch.from_numpy(V0), torch.from_numpy(F), pid)
+    out = PD.RigidEdgeLoss_forward(torch.from_numpy(V0).to(cuda), torch.from_numpy(F).to(cuda), pid)
+    assert out.shape == (0, 3)
+    g = PD.RigidEdgeLoss_backward(torch.from_numpy(V0).to(cuda), torch.from_numpy(F).to(cuda), pid)
+    assert torch.all(g == 0)
