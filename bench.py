@@ -1,0 +1,389 @@
+#!/usr/bin/env python
+"""Headline benchmark: the mixed 512-request deformation serving stream.
+
+Workload (synthetic, seeded; the reference publishes no benchmark data):
+512 requests, source vertices log-uniform in [2k, 100k] (cube-spheres),
+target triangles log-uniform in [5k, 500k] (displaced cube-spheres), grid 64^3
+or 128^3 (50/50), 500 Adam steps each (lr 1e-3), numpy PCG64(seed=5); each
+request is one run of the reference's rigid_deform loop (normalise by the
+target, build its distance field, DistanceFieldLoss + RigidEdgeLoss + Adam,
+denormalise).
+
+One bench step = the whole 512-request stream served to completion by the
+continuous-batching engine, all requests offered at the start (saturating
+load).  ``value`` = pair-solves/s with the meshes already resident in HBM;
+``e2e`` = the same through the public API with pinned host meshes copied in
+and fitted meshes copied out inside the timed region.  Also reported: p50/p95/
+p99 latency under Poisson arrivals at 200 requests/s, the plain one-pair-at-
+a-time GPU loop (the reference loop over the GPU pyDeform + torch.optim.Adam)
+and the CPU path (the oracle restatement of pyDeform + torch CPU Adam) on
+bounded samples, and the fused step's HBM roofline.
+
+``--impl reference`` times the reference's CPU implementation of the path
+(the oracle port; the reference itself cannot be built here) on the host
+cores, one bounded sample of the stream per step.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+import torch  # noqa: E402
+
+METRIC = "pair-solves/s (batched serving, 512-request mixed stream)"
+UNIT = "pair-solves/s"
+WORKLOAD = "serving-stream-512 (V logU[2k,100k], T logU[5k,500k], N 64|128, 500 steps)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--requests", type=int, default=512)
+    ap.add_argument("--req-steps", type=int, default=500)
+    ap.add_argument("--group-steps", type=int, default=25)
+    ap.add_argument("--plain-sample", type=int, default=6)
+    ap.add_argument("--cpu-sample-s", type=float, default=20.0)
+    ap.add_argument("--no-extras", action="store_true", help="skip latency/plain/cpu legs")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (replicas: each rank serves its own stream)
+# ---------------------------------------------------------------------------
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return world, rank
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world <= 1:
+        return x
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled with nvidia-smi during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+                power.append(float(p[3]))
+            except ValueError:
+                continue
+            for name, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "power_w_max": float(max(power)),
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+def make_stream(args, seed):
+    from meshode_gb300 import meshgen
+    specs = meshgen.serving_requests(n=args.requests, seed=seed, steps=args.req_steps)
+    meshes = [meshgen.request_meshes(s) for s in specs]
+    return specs, meshes
+
+
+def cpu_sample_ids(specs, k=2, seed=7):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return sorted(rng.choice(len(specs), size=min(k, len(specs)), replace=False).tolist())
+
+
+def run_cpu_port(specs, meshes, ids, threads):
+    """The oracle restatement of the reference's CPU path for the listed
+    requests: FP64 DF through an AABB tree, then the rigid_deform loop with
+    the restated pyDeform losses and torch.optim.Adam on the CPU."""
+    from oracle import pydeform_oracle as orc
+    torch.set_num_threads(threads)
+    t0 = time.perf_counter()
+    outs = []
+    for i in ids:
+        Vs, Fs, Vt, Ft = meshes[i]
+        pid = orc.InitializeDeformTemplate(Vt, Ft, 0, specs[i]["N"])
+        V = torch.from_numpy(Vs.copy())
+        orc.NormalizeByTemplate(V, pid)
+        Ft_ = torch.from_numpy(Fs)
+        orc.StoreRigidityInformation(V, Ft_, pid)
+        out, _ = orc.rigid_fit(V, Ft_, pid, specs[i]["steps"])
+        outs.append(out)
+    return time.perf_counter() - t0, outs
+
+
+def run_plain_gpu(specs, meshes, ids):
+    """The reference's loop verbatim (rigid_deform.py:25-41) over the GPU
+    pyDeform, one pair at a time, torch.optim.Adam on CUDA."""
+    from meshode_gb300 import layers
+    dev = torch.device("cuda")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    outs = []
+    for i in ids:
+        Vs, Fs, Vt, Ft = meshes[i]
+        src_V = torch.from_numpy(Vs).to(dev)
+        src_F = torch.from_numpy(Fs).to(dev)
+        layer = layers.RigidLossLayer(src_V, src_F, torch.from_numpy(Vt).to(dev), torch.from_numpy(Ft).to(dev),
+                                      grid_resolution=specs[i]["N"])
+        P = torch.nn.Parameter(src_V)
+        opt = torch.optim.Adam([P], lr=1e-3)
+        for _ in range(specs[i]["steps"]):
+            opt.zero_grad()
+            loss = layer(P, src_F)
+            loss.backward()
+            opt.step()
+        outs.append(P.detach().clone())
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0, outs
+
+
+# ---------------------------------------------------------------------------
+def reference_arm(args, world, rank):
+    """CPU implementation of the path (oracle port), all host threads."""
+    if rank != 0:
+        return
+    specs, meshes = make_stream(argparse.Namespace(requests=args.requests, req_steps=args.req_steps), 5)
+    ids = cpu_sample_ids(specs)
+    threads = os.cpu_count() or 1
+    from oracle import build as ob
+    ob.build()
+    for _ in range(args.warmup):
+        run_cpu_port(specs, meshes, ids[:1], threads)
+    times = []
+    for _ in range(args.steps):
+        dt, _ = run_cpu_port(specs, meshes, ids, threads)
+        times.append(dt)
+    t = float(np.mean(times))
+    value = len(ids) / t
+    sample = "requests %s of the 512-request stream (DF build + %d Adam steps each) per step" % (ids, args.req_steps)
+    print(json.dumps({
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def ours_arm(args, world, rank):
+    from meshode_gb300 import _lib as L
+    from meshode_gb300 import metrics, serving
+    from meshode_gb300 import build as B
+    B.build()
+    L.require_cuda()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    specs, meshes = make_stream(args, 5 + rank)
+    lib = L.lib()
+    req_dev = serving.requests_from_meshes(meshes, specs, device=dev)
+    req_host = serving.requests_from_meshes(meshes, specs, device=None, pin=True)
+    h2d = sum(sum(a.nbytes for a in m) for m in meshes)
+    d2h = sum(m[0].nbytes for m in meshes)
+    torch.cuda.synchronize()
+
+    def fresh(reqs):
+        return [serving.Request(r.id, r.srcV, r.srcF, r.tarV, r.tarF, N=r.N, steps=r.steps, arrival=r.arrival)
+                for r in reqs]
+
+    engine = serving.ServingEngine(device=dev, group_steps=args.group_steps, results_to_host=False)
+    for _ in range(args.warmup):
+        engine.run(fresh(req_dev))
+    engine.group_time_s = engine.group_bytes = 0.0
+    # ---- timed: device-resident inputs ----
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    n0 = lib.mo_launch_count()
+    g0 = engine.runner.launches
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    last = None
+    for _ in range(args.steps):
+        last = fresh(req_dev)
+        engine.run(last)
+    ev1.record()
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    t_dev = ev0.elapsed_time(ev1) * 1e-3
+    launches = (lib.mo_launch_count() - n0) + (engine.runner.launches - g0 if engine.runner.use_graph else 0)
+    t_max = max_over_ranks(t_dev, world)
+    value = world * args.requests * args.steps / t_max
+    achieved, step_s = engine.step_roofline()
+    # ---- timed: end to end through host buffers ----
+    engine_h = serving.ServingEngine(device=dev, group_steps=args.group_steps, results_to_host=True)
+    engine_h.run(fresh(req_host))  # warm-up of this engine (graph capture)
+    barrier(world)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        engine_h.run(fresh(req_host))
+    e1.record()
+    torch.cuda.synchronize()
+    barrier(world)
+    t_e2e = max_over_ranks(e0.elapsed_time(e1) * 1e-3, world)
+    e2e_value = world * args.requests * args.steps / t_e2e
+    if rank != 0:
+        return
+    extras = {}
+    if not args.no_extras:
+        # latency under Poisson arrivals at 200 requests/s
+        lat_reqs = fresh(req_dev)
+        engine.run(lat_reqs, realtime=True)
+        lats = np.asarray([r.latency for r in lat_reqs]) * 1e3
+        extras["latency_ms"] = {"p50": float(np.percentile(lats, 50)), "p95": float(np.percentile(lats, 95)),
+                                "p99": float(np.percentile(lats, 99)), "arrivals": "poisson 200 req/s"}
+        extras["saturated_latency_ms_p99"] = float(np.percentile(
+            np.asarray([r.latency for r in last]) * 1e3, 99))
+        # plain one-pair-at-a-time GPU loop on a bounded sample
+        ids = list(range(min(args.plain_sample, len(specs))))
+        t_plain, plain_out = run_plain_gpu(specs, meshes, ids)
+        plain_rate = len(ids) / t_plain
+        extras["plain_gpu"] = {"value": plain_rate, "unit": UNIT, "sample": "requests %s, sequential" % ids,
+                               "batched_over_plain": value / plain_rate}
+        # matched Chamfer on the sample (target-normalised unit cube)
+        diffs = []
+        for j, i in enumerate(ids):
+            Vs, Fs, Vt, Ft = meshes[i]
+            from oracle import pydeform_oracle as orc  # checker only
+            sc, tr = orc.normalize_params(Vt)
+            Tn = orc.normalized_double(Vt, sc, tr)
+            a = last[i].out_normalized.cpu().numpy()
+            b = plain_out[j].cpu().numpy()
+            ca = metrics.chamfer(a, Fs, Tn, Ft, samples=20000)
+            cb = metrics.chamfer(b, Fs, Tn, Ft, samples=20000)
+            diffs.append(abs(ca - cb))
+        extras["chamfer_vs_plain_max_abs_diff"] = float(max(diffs))
+        # CPU path on a bounded sample
+        threads = os.cpu_count() or 1
+        cids = cpu_sample_ids(specs, k=1)
+        t_cpu, cpu_out = run_cpu_port(specs, meshes, cids, threads)
+        cpu_rate = len(cids) / t_cpu
+        i = cids[0]
+        sc, tr = orc.normalize_params(meshes[i][2])
+        Tn = orc.normalized_double(meshes[i][2], sc, tr)
+        c_cpu = metrics.chamfer(cpu_out[0].numpy(), meshes[i][1], Tn, meshes[i][3], samples=20000)
+        c_gpu = metrics.chamfer(last[i].out_normalized.cpu().numpy(), meshes[i][1], Tn, meshes[i][3], samples=20000)
+        extras["chamfer_vs_cpu_abs_diff"] = abs(c_cpu - c_gpu)
+        cpu_baseline = {"value": cpu_rate, "unit": UNIT, "cores": threads, "kind": "port",
+                        "sample": "request %s (DF build + %d steps), oracle restatement + torch CPU Adam"
+                                  % (cids, args.req_steps)}
+    else:
+        cpu_baseline = None
+    peak, peak_kind = measured_peaks()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "requests": args.requests, "req_steps": args.req_steps,
+                   "group_steps": args.group_steps, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "inputs larger than L2 (~1.3 GB meshes, ~20 GB grids per stream)"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "kernel": "k_fused_step", "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "bytes_formula": "104*V + 44*H per pair-step", "step_seconds": step_s},
+        "cpu_baseline": cpu_baseline,
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+    line.update(extras)
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    world, rank = dist_setup(args)
+    if args.impl == "reference":
+        reference_arm(args, world, rank)
+    else:
+        ours_arm(args, world, rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -46,6 +46,9 @@ extern "C" {
 const char* mo_last_error(void);
 /* Library ABI version (major*100 + minor). */
 int mo_version(void);
+/* Kernel launches issued by this library since it was loaded (launches
+ * replayed from a captured CUDA graph are not included). */
+unsigned long long mo_launch_count(void);
 
 /* ------------------------------------------------------------------------
  * Normalisation by the target's transform.

@@ -43,6 +43,7 @@ class MoTile(ctypes.Structure):
 _SIGS = {
     "mo_last_error": (ctypes.c_char_p, []),
     "mo_version": (_I, []),
+    "mo_launch_count": (ctypes.c_ulonglong, []),
     "mo_bbox": (_I, [_P, _I64, _P, _P]),
     "mo_norm_params": (_I, [_P, _P, _P]),
     "mo_normalize": (_I, [_P, _I64, _P, _I, _P]),

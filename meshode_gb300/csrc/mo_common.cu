@@ -1,5 +1,6 @@
 // Error state, device queries and two set-up primitives shared by the
 // builders: a single-CTA exclusive scan and a stable LSD radix sort.
+#include <atomic>
 #include <cstdarg>
 #include <cstring>
 
@@ -8,6 +9,9 @@
 namespace mo {
 
 static thread_local char g_err[512] = "";
+static std::atomic<unsigned long long> g_launches{0};
+
+void note_launch(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
 
 void set_error(const char* fmt, ...) {
     va_list ap;
@@ -70,7 +74,7 @@ cudaError_t exclusive_scan_i32(int* data, int n, int* total, cudaStream_t s) {
         if (total) return cudaMemsetAsync(total, 0, sizeof(int), s);
         return cudaSuccess;
     }
-    k_scan_1cta<<<1, 1024, 0, s>>>(data, n, total);
+    k_scan_1cta<<<1, 1024, 0, s>>>(data, n, total); ::mo::note_launch();
     return cudaGetLastError();
 }
 
@@ -155,10 +159,10 @@ cudaError_t radix_sort_pairs(uint32_t* keys_a, int* vals_a, uint32_t* keys_b, in
     int *vi = vals_a, *vo = vals_b;
     for (int p = 0; p < passes; ++p) {
         const int shift = 8 * p;
-        k_rs_hist<<<ntiles, 256, 0, s>>>(ki, n, shift, hist, ntiles);
+        k_rs_hist<<<ntiles, 256, 0, s>>>(ki, n, shift, hist, ntiles); ::mo::note_launch();
         cudaError_t e = exclusive_scan_i32(hist, 256 * ntiles, nullptr, s);
         if (e != cudaSuccess) return e;
-        k_rs_scatter<<<ntiles, 256, 0, s>>>(ki, vi, ko, vo, n, shift, hist, ntiles);
+        k_rs_scatter<<<ntiles, 256, 0, s>>>(ki, vi, ko, vo, n, shift, hist, ntiles); ::mo::note_launch();
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         uint32_t* tk = ki; ki = ko; ko = tk;
@@ -177,3 +181,4 @@ cudaError_t radix_sort_pairs(uint32_t* keys_a, int* vals_a, uint32_t* keys_b, in
 
 extern "C" const char* mo_last_error(void) { return mo::g_err; }
 extern "C" int mo_version(void) { return 100; }
+extern "C" unsigned long long mo_launch_count(void) { return mo::g_launches.load(std::memory_order_relaxed); }

@@ -75,6 +75,9 @@ inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
 int device_sm_count();
 
+// Counts kernel launches issued through this library (mo_launch_count()).
+void note_launch(int n = 1);
+
 // Exclusive scan of n ints in place (single CTA; used for one-shot set-up
 // arrays).  If total != nullptr, the sum is stored there (device pointer).
 cudaError_t exclusive_scan_i32(int* data, int n, int* total, cudaStream_t s);

@@ -487,10 +487,10 @@ extern "C" int mo_bbox(const float* V, int64_t n, int32_t* bbox6, void* stream) 
     MO_CHECK_ARG(n >= 0, "negative vertex count");
     MO_CHECK_ARG(bbox6 && (n == 0 || V), "null pointer");
     cudaStream_t s = as_stream(stream);
-    k_bbox_init<<<1, 32, 0, s>>>(bbox6);
+    k_bbox_init<<<1, 32, 0, s>>>(bbox6); ::mo::note_launch();
     if (n > 0) {
         const int blocks = std::min(ceil_div(n, 256), 4 * device_sm_count());
-        k_bbox<<<blocks, 256, 0, s>>>(V, n, bbox6);
+        k_bbox<<<blocks, 256, 0, s>>>(V, n, bbox6); ::mo::note_launch();
     }
     MO_LAUNCH_CHECK("k_bbox");
     return MO_OK;
@@ -498,7 +498,7 @@ extern "C" int mo_bbox(const float* V, int64_t n, int32_t* bbox6, void* stream) 
 
 extern "C" int mo_norm_params(const int32_t* bbox6, double* params4, void* stream) {
     MO_CHECK_ARG(bbox6 && params4, "null pointer");
-    k_norm_params<<<1, 1, 0, as_stream(stream)>>>(bbox6, params4);
+    k_norm_params<<<1, 1, 0, as_stream(stream)>>>(bbox6, params4); ::mo::note_launch();
     MO_LAUNCH_CHECK("k_norm_params");
     return MO_OK;
 }
@@ -507,7 +507,7 @@ extern "C" int mo_normalize(float* V, int64_t n, const double* params4, int inve
     MO_CHECK_ARG(n >= 0, "negative vertex count");
     if (n == 0) return MO_OK;
     MO_CHECK_ARG(V && params4, "null pointer");
-    k_normalize<<<ceil_div(3 * n, 256), 256, 0, as_stream(stream)>>>(V, n, params4, inverse);
+    k_normalize<<<ceil_div(3 * n, 256), 256, 0, as_stream(stream)>>>(V, n, params4, inverse); ::mo::note_launch();
     MO_LAUNCH_CHECK("k_normalize");
     return MO_OK;
 }
@@ -557,24 +557,24 @@ extern "C" int mo_df_build(const float* V, int64_t nv, const int32_t* F, int64_t
             e = cudaMemsetAsync(S.status, 0, sizeof(int) * 4, s);
             if (e != cudaSuccess) { fail(e, "memset"); break; }
         }
-        k_normalize_copy<<<ceil_div(3 * nv, 256), 256, 0, s>>>(V, nv, params4, S.Vn);
+        k_normalize_copy<<<ceil_div(3 * nv, 256), 256, 0, s>>>(V, nv, params4, S.Vn); ::mo::note_launch();
         if (method == MO_DF_BRUTE) {
-            k_check_faces<<<ceil_div(nf, 256), 256, 0, s>>>(F, nf, nv, st);
-            k_tri_records<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, nullptr, S.tris);
+            k_check_faces<<<ceil_div(nf, 256), 256, 0, s>>>(F, nf, nv, st); ::mo::note_launch();
+            k_tri_records<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, nullptr, S.tris); ::mo::note_launch();
             const int64_t nvox = (int64_t)N * N * N;
-            k_df_brute<<<ceil_div(nvox, BF_THREADS), BF_THREADS, 0, s>>>(S.tris, (int)nf, N, grid_out);
+            k_df_brute<<<ceil_div(nvox, BF_THREADS), BF_THREADS, 0, s>>>(S.tris, (int)nf, N, grid_out); ::mo::note_launch();
         } else {
-            k_morton<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.codes_a, S.ids_a, st);
+            k_morton<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.codes_a, S.ids_a, st); ::mo::note_launch();
             e = radix_sort_pairs(S.codes_a, S.ids_a, S.codes_b, S.ids_b, (int)nf, 30, S.hist, s);
             if (e != cudaSuccess) { fail(e, "radix_sort_pairs"); break; }
-            k_tri_records<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.ids_a, S.tris);
+            k_tri_records<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.ids_a, S.tris); ::mo::note_launch();
             if (nf > 1) {
-                k_karras<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.codes_a, (int)nf, S.nodes, S.parent, S.flags);
-                k_refit<<<ceil_div(nf, 256), 256, 0, s>>>(S.tris, (int)nf, S.nodes, S.parent, S.flags, S.rootbox, st);
+                k_karras<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.codes_a, (int)nf, S.nodes, S.parent, S.flags); ::mo::note_launch();
+                k_refit<<<ceil_div(nf, 256), 256, 0, s>>>(S.tris, (int)nf, S.nodes, S.parent, S.flags, S.rootbox, st); ::mo::note_launch();
             }
             const int64_t bricks = (int64_t)((N + 3) / 4) * ((N + 3) / 4) * ((N + 1) / 2);
             k_df_lbvh<<<ceil_div(bricks, TRAV_WARPS), TRAV_WARPS * 32, 0, s>>>(S.nodes, S.tris, (int)nf, N,
-                                                                               grid_out, st);
+                                                                               grid_out, st); ::mo::note_launch();
         }
         e = cudaGetLastError();
         if (e != cudaSuccess) { fail(e, "df build kernels"); break; }
@@ -613,16 +613,16 @@ extern "C" int mo_lbvh_build(const float* V, int64_t nv, const int32_t* F, int64
     int rc = MO_OK;
     cudaError_t e = cudaMemsetAsync(S.status, 0, sizeof(int) * 4, s);
     if (e == cudaSuccess) {
-        k_normalize_copy<<<ceil_div(3 * nv, 256), 256, 0, s>>>(V, nv, params4, S.Vn);
-        k_morton<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.codes_a, S.ids_a, S.status);
+        k_normalize_copy<<<ceil_div(3 * nv, 256), 256, 0, s>>>(V, nv, params4, S.Vn); ::mo::note_launch();
+        k_morton<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.codes_a, S.ids_a, S.status); ::mo::note_launch();
         e = radix_sort_pairs(S.codes_a, S.ids_a, S.codes_b, S.ids_b, (int)nf, 30, S.hist, s);
     }
     if (e == cudaSuccess) {
-        k_tri_records<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.ids_a, S.tris);
+        k_tri_records<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.ids_a, S.tris); ::mo::note_launch();
         if (nf > 1) {
-            k_karras<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.codes_a, (int)nf, S.nodes, S.parent, S.flags);
+            k_karras<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.codes_a, (int)nf, S.nodes, S.parent, S.flags); ::mo::note_launch();
             k_refit<<<ceil_div(nf, 256), 256, 0, s>>>(S.tris, (int)nf, S.nodes, S.parent, S.flags, S.rootbox,
-                                                      S.status);
+                                                      S.status); ::mo::note_launch();
         }
         e = cudaGetLastError();
     }

@@ -42,12 +42,14 @@ static int launch_dfloss(const float* V, int64_t n, const float* grid, int N, in
     const int threads = 256;
     const int blocks = ceil_div(n, threads);
     const float Nf = (float)N, Cf = far_offset(N);
-    if (layout == MO_LAYOUT_CELL)
+    if (layout == MO_LAYOUT_CELL) {
         k_dfloss<MO_LAYOUT_CELL, FWD, BWD><<<blocks, threads, 0, s>>>(V, n, grid, N, Nf, Cf, loss, grad,
                                                                       use_mask, mask_thresh);
-    else
+    } else {
         k_dfloss<MO_LAYOUT_LINEAR, FWD, BWD><<<blocks, threads, 0, s>>>(V, n, grid, N, Nf, Cf, loss, grad,
                                                                         use_mask, mask_thresh);
+    }
+    ::mo::note_launch();
     MO_LAUNCH_CHECK("k_dfloss");
     return MO_OK;
 }
@@ -104,7 +106,7 @@ extern "C" int mo_grid_relayout(const float* grid_linear, int N, int layout, flo
     MO_CHECK_ARG(layout == MO_LAYOUT_CELL, "unknown grid layout %d", layout);
     MO_CHECK_ARG(aligned(out, 16), "cell-layout output must be 16-byte aligned");
     const int64_t M = N - 1, cells = M * M * M;
-    k_relayout_cell<<<ceil_div(cells, 256), 256, 0, s>>>(grid_linear, N, reinterpret_cast<float4*>(out));
+    k_relayout_cell<<<ceil_div(cells, 256), 256, 0, s>>>(grid_linear, N, reinterpret_cast<float4*>(out)); ::mo::note_launch();
     MO_LAUNCH_CHECK("k_relayout_cell");
     return MO_OK;
 }

@@ -222,7 +222,7 @@ extern "C" int mo_edge_offsets(const float* V, int64_t nv, const int32_t* idx, i
     if (rc) return rc;
     if (nh == 0) return MO_OK;
     MO_CHECK_ARG(off_out, "null output pointer");
-    k_edge_offsets<<<ceil_div(nh, 256), 256, 0, as_stream(stream)>>>(V, nv, idx, nh, kind, off_out);
+    k_edge_offsets<<<ceil_div(nh, 256), 256, 0, as_stream(stream)>>>(V, nv, idx, nh, kind, off_out); ::mo::note_launch();
     MO_LAUNCH_CHECK("k_edge_offsets");
     return MO_OK;
 }
@@ -234,7 +234,7 @@ extern "C" int mo_edge_forward(const float* V, int64_t nv, const int32_t* idx, i
     if (rc) return rc;
     if (nh == 0) return MO_OK;
     MO_CHECK_ARG(off && loss_out, "null offset or output pointer");
-    k_edge_forward<<<ceil_div(nh, 256), 256, 0, as_stream(stream)>>>(V, nv, idx, nh, kind, off, loss_out);
+    k_edge_forward<<<ceil_div(nh, 256), 256, 0, as_stream(stream)>>>(V, nv, idx, nh, kind, off, loss_out); ::mo::note_launch();
     MO_LAUNCH_CHECK("k_edge_forward");
     return MO_OK;
 }
@@ -261,16 +261,16 @@ extern "C" int mo_edge_csr_build(const int32_t* idx, int64_t n_items, int kind, 
     MO_CUDA(cudaMemsetAsync(c.cursor, 0, sizeof(int) * (nv + 1), s));  // cursor[nv] + status
     int* st = status_out ? reinterpret_cast<int*>(status_out) : c.status;
     if (nh > 0) {
-        k_csr_count<<<ceil_div(nh, 256), 256, 0, s>>>(idx, nh, kind, nv, c.row_ptr, st);
+        k_csr_count<<<ceil_div(nh, 256), 256, 0, s>>>(idx, nh, kind, nv, c.row_ptr, st); ::mo::note_launch();
         MO_LAUNCH_CHECK("k_csr_count");
     }
     MO_CUDA(exclusive_scan_i32(c.row_ptr, (int)(nv + 1), nullptr, s));
     if (nh > 0) {
-        k_csr_fill<<<ceil_div(nh, 256), 256, 0, s>>>(idx, nh, kind, nv, c.row_ptr, c.cursor, c.key, c.other);
+        k_csr_fill<<<ceil_div(nh, 256), 256, 0, s>>>(idx, nh, kind, nv, c.row_ptr, c.cursor, c.key, c.other); ::mo::note_launch();
         MO_LAUNCH_CHECK("k_csr_fill");
     }
     if (nv > 0) {
-        k_csr_sort_rows<<<ceil_div(nv, 256), 256, 0, s>>>(nv, c.row_ptr, c.key, c.other);
+        k_csr_sort_rows<<<ceil_div(nv, 256), 256, 0, s>>>(nv, c.row_ptr, c.key, c.other); ::mo::note_launch();
         MO_LAUNCH_CHECK("k_csr_sort_rows");
     }
     if (status_out) return MO_OK;
@@ -291,7 +291,7 @@ extern "C" int mo_edge_backward(const float* V, int64_t nv, const void* csr, int
     MO_CHECK_ARG(V && csr && grad_out && (nh == 0 || off), "null pointer");
     CsrView c = csr_view(const_cast<void*>(csr), nv, nh);
     k_edge_backward<<<ceil_div(nv, 256), 256, 0, as_stream(stream)>>>(V, nv, c.row_ptr, c.key, c.other, off,
-                                                                      grad_out);
+                                                                      grad_out); ::mo::note_launch();
     MO_LAUNCH_CHECK("k_edge_backward");
     return MO_OK;
 }
@@ -304,7 +304,7 @@ extern "C" int mo_sell_plan(const void* csr, int64_t nv, int64_t nh, int32_t* sl
     CsrView c = csr_view(const_cast<void*>(csr), nv, nh);
     MO_CUDA(cudaMemsetAsync(slice_ptr, 0, sizeof(int) * (nslices + 1), s));
     if (nslices > 0) {
-        k_sell_width<<<ceil_div(nslices * 32, 256), 256, 0, s>>>(nv, nslices, c.row_ptr, slice_ptr);
+        k_sell_width<<<ceil_div(nslices * 32, 256), 256, 0, s>>>(nv, nslices, c.row_ptr, slice_ptr); ::mo::note_launch();
         MO_LAUNCH_CHECK("k_sell_width");
     }
     MO_CUDA(exclusive_scan_i32(slice_ptr, (int)(nslices + 1), nullptr, s));
@@ -320,7 +320,7 @@ extern "C" int mo_sell_fill(const void* csr, int64_t nv, int64_t nh, const float
     const int64_t nslices = (nv + 31) / 32;
     CsrView c = csr_view(const_cast<void*>(csr), nv, nh);
     k_sell_fill<<<ceil_div(nslices * 32, 256), 256, 0, as_stream(stream)>>>(
-        nv, nslices, c.row_ptr, c.key, c.other, off, slice_ptr, reinterpret_cast<float4*>(records));
+        nv, nslices, c.row_ptr, c.key, c.other, off, slice_ptr, reinterpret_cast<float4*>(records)); ::mo::note_launch();
     MO_LAUNCH_CHECK("k_sell_fill");
     return MO_OK;
 }

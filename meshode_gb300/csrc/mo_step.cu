@@ -181,7 +181,7 @@ extern "C" int mo_adam_step(float* P, const float* G, float* M, float* Vsq, int6
     if (n == 0) return MO_OK;
     MO_CHECK_ARG(P && G && M && Vsq, "null pointer");
     k_adam<<<ceil_div(n, 256), 256, 0, as_stream(stream)>>>(P, G, M, Vsq, n, one_minus_b1, b2, one_minus_b2, eps,
-                                                           step_size, bc2_sqrt);
+                                                           step_size, bc2_sqrt); ::mo::note_launch();
     MO_LAUNCH_CHECK("k_adam");
     return MO_OK;
 }
@@ -194,7 +194,7 @@ extern "C" int mo_fused_step(const MoPair* pairs, const MoTile* tiles, const int
     int ctas = grid_ctas > 0 ? grid_ctas : step_ctas();
     if (ctas > max_tiles) ctas = max_tiles;
     k_fused_step<<<ctas, STEP_THREADS, 0, as_stream(stream)>>>(pairs, tiles, ntiles, max_tiles, launch_index,
-                                                              tile_loss);
+                                                              tile_loss); ::mo::note_launch();
     MO_LAUNCH_CHECK("k_fused_step");
     return MO_OK;
 }
@@ -206,7 +206,7 @@ extern "C" int mo_pair_loss(const MoPair* pairs, int npairs, int max_tiles, int 
     if (n == 0) return MO_OK;
     MO_CHECK_ARG(pairs && tile_loss && pair_loss, "null pointer");
     k_pair_loss<<<ceil_div(n, 128), 128, 0, as_stream(stream)>>>(pairs, npairs, max_tiles, nlaunch, tile_loss,
-                                                                pair_loss);
+                                                                pair_loss); ::mo::note_launch();
     MO_LAUNCH_CHECK("k_pair_loss");
     return MO_OK;
 }
@@ -215,7 +215,7 @@ extern "C" int mo_pack_pos(const float* V, int64_t n, float* pos4, void* stream)
     MO_CHECK_ARG(n >= 0, "negative size");
     if (n == 0) return MO_OK;
     MO_CHECK_ARG(V && pos4 && aligned(pos4, 16), "null or misaligned pointer");
-    k_pack<<<ceil_div(n, 256), 256, 0, as_stream(stream)>>>(V, n, reinterpret_cast<float4*>(pos4));
+    k_pack<<<ceil_div(n, 256), 256, 0, as_stream(stream)>>>(V, n, reinterpret_cast<float4*>(pos4)); ::mo::note_launch();
     MO_LAUNCH_CHECK("k_pack");
     return MO_OK;
 }
@@ -224,7 +224,7 @@ extern "C" int mo_unpack_pos(const float* pos4, int64_t n, float* V, void* strea
     MO_CHECK_ARG(n >= 0, "negative size");
     if (n == 0) return MO_OK;
     MO_CHECK_ARG(V && pos4 && aligned(pos4, 16), "null or misaligned pointer");
-    k_unpack<<<ceil_div(n, 256), 256, 0, as_stream(stream)>>>(reinterpret_cast<const float4*>(pos4), n, V);
+    k_unpack<<<ceil_div(n, 256), 256, 0, as_stream(stream)>>>(reinterpret_cast<const float4*>(pos4), n, V); ::mo::note_launch();
     MO_LAUNCH_CHECK("k_unpack");
     return MO_OK;
 }

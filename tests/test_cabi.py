@@ -13,7 +13,7 @@ HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))
 def declared_functions():
     src = open(HEADER).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\*?\s*(mo_[A-Za-z0-9_]+)\s*\(", src, flags=re.M)
+    names = re.findall(r"^\s*(?:[A-Za-z_][A-Za-z0-9_]*[\s*]+)+(mo_[A-Za-z0-9_]+)\s*\(", src, flags=re.M)
     return sorted(set(names))
 
 
