@@ -88,6 +88,25 @@ int mo_df_build(const float* V, int64_t nv, const int32_t* F, int64_t nf, int N,
 int mo_lbvh_build(const float* V, int64_t nv, const int32_t* F, int64_t nf, const double* params4,
                   void* scratch, size_t scratch_bytes, uint32_t* sorted_codes, int32_t* order,
                   int32_t* left, int32_t* right, float* root_box, void* stream);
+/* Allocation-free variant of mo_df_build, for callers that cannot allocate
+ * device memory while they run (a plugin inside a host runtime that owns the
+ * device memory pool, a real-time loop that forbids allocation after
+ * start-up).  No counterpart in the reference.  The build's scratch is one
+ * fixed device array of MO_DF_NOALLOC_SCRATCH_BYTES that every GPU loading
+ * this library holds until the process exits; targets whose scratch need
+ * (mo_df_build_scratch_bytes with mo_df_method_for's method) exceeds it are
+ * rejected with MO_ERR_SCRATCH -- about 50,000 triangles.  The caller still
+ * passes the inputs and the output grid.  The first call on a device, made
+ * with that device current, looks up the array's device address; make that
+ * first call before any stream capture.  Every call shares the array and
+ * leaves its contents behind: calls that overlap on the GPU (other streams,
+ * other host threads) race and must be serialised by the caller.  The call
+ * synchronises `stream` to read the build status. */
+#define MO_DF_NOALLOC_SCRATCH_BYTES (8u << 20)
+int mo_df_build_noalloc(const float* V, int64_t nv, const int32_t* F, int64_t nf, int N,
+                        const double* params4, float* grid_linear_out, void* stream);
+/* MO_DF_NOALLOC_SCRATCH_BYTES as compiled into the library. */
+size_t mo_df_noalloc_scratch_capacity(void);
 /* Method MO_DF_AUTO resolves to (host-side heuristic, exported for tests). */
 int mo_df_method_for(int64_t nf, int N);
 

@@ -50,6 +50,8 @@ _SIGS = {
     "mo_df_build_scratch_bytes": (_SZ, [_I64, _I64, _I, _I]),
     "mo_df_build": (_I, [_P, _I64, _P, _I64, _I, _P, _I, _P, _SZ, _P, _P, _P]),
     "mo_df_method_for": (_I, [_I64, _I]),
+    "mo_df_build_noalloc": (_I, [_P, _I64, _P, _I64, _I, _P, _P, _P]),
+    "mo_df_noalloc_scratch_capacity": (_SZ, []),
     "mo_lbvh_build": (_I, [_P, _I64, _P, _I64, _P, _P, _SZ, _P, _P, _P, _P, _P, _P]),
     "mo_grid_bytes": (_SZ, [_I, _I]),
     "mo_grid_relayout": (_I, [_P, _I, _I, _P, _P]),

@@ -6,6 +6,7 @@
 // igl::point_mesh_squared_distance query (mesh.cc:140) returns the exact
 // squared distance to the nearest triangle; the grid stores its sqrt.
 #include <cfloat>
+#include <mutex>
 
 #include "mo_common.cuh"
 
@@ -648,4 +649,68 @@ extern "C" int mo_lbvh_build(const float* V, int64_t nv, const int32_t* F, int64
     }
     if (owned) cudaFreeAsync(owned, s);
     return rc;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free distance-field build.
+//
+// Some callers cannot allocate device memory while they run: code executing
+// inside another runtime or plugin host that owns the whole device memory
+// pool, or a real-time loop whose policy forbids allocation after start-up.
+// For them the build's scratch lives in one fixed, file-scope device array
+// that every GPU loading this library holds until the process exits.
+// In host code the array's name is only a host-side stand-in; its device
+// address is looked up once per device with cudaGetSymbolAddress.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_df_noalloc_scratch[MO_DF_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[kMaxDevices] = {};
+}  // namespace
+
+// Device address of the fixed scratch on the current device (looked up on the
+// first call made with that device current).
+static int noalloc_scratch_address(void** out) {
+    int dev = 0;
+    MO_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) {
+        set_error("device ordinal %d is outside the %d devices this library tracks", dev, kMaxDevices);
+        return MO_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_df_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_df_noalloc_scratch)");
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return MO_OK;
+}
+
+extern "C" size_t mo_df_noalloc_scratch_capacity(void) { return MO_DF_NOALLOC_SCRATCH_BYTES; }
+
+extern "C" int mo_df_build_noalloc(const float* V, int64_t nv, const int32_t* F, int64_t nf, int N,
+                                   const double* params4, float* grid_linear_out, void* stream) {
+    MO_CHECK_ARG(nv > 0 && nf > 0, "target mesh must have vertices and faces (nv=%lld nf=%lld)", (long long)nv,
+                 (long long)nf);
+    MO_CHECK_ARG(nf < ((int64_t)1 << 30) && nv < ((int64_t)1 << 31), "target mesh too large");
+    MO_CHECK_ARG(N >= 2 && N <= 2048, "grid resolution out of range (%d)", N);
+    const int method = mo_df_method_for(nf, N);
+    const size_t need = plan_scratch(nullptr, nv, nf, method).bytes;
+    if (need > (size_t)MO_DF_NOALLOC_SCRATCH_BYTES) {
+        set_error("mo_df_build_noalloc: a target with %lld vertices and %lld faces needs %zu bytes of scratch, "
+                  "more than the fixed %zu-byte array; use mo_df_build with caller scratch",
+                  (long long)nv, (long long)nf, need, (size_t)MO_DF_NOALLOC_SCRATCH_BYTES);
+        return MO_ERR_SCRATCH;
+    }
+    void* scratch = nullptr;
+    const int rc = noalloc_scratch_address(&scratch);
+    if (rc != MO_OK) return rc;
+    // status_out == NULL: the build reads its status word from the fixed
+    // array (zeroed at the start of every call) and synchronises `stream`.
+    return mo_df_build(V, nv, F, nf, N, params4, method, scratch, (size_t)MO_DF_NOALLOC_SCRATCH_BYTES,
+                       grid_linear_out, nullptr, stream);
 }
