@@ -164,14 +164,17 @@ int mo_edge_backward(const float* V, int64_t nv, const void* csr, int64_t nh, co
                      float* grad_out, void* stream);
 
 /* Sliced-ELL (32-vertex slices, column-major records) view of the CSR for
- * the fused step: records are float4 {other | role<<31, off.x, off.y, off.z},
- * padding records have other == -1.  slice_ptr is int32[ceil(nv/32)+1];
+ * the fused step: one int32 record per incident half-edge, other | role<<31
+ * (role 1 when the vertex is the half-edge's v1), in half-edge order;
+ * padding records are -1.  The fused step recomputes each rest offset as
+ * rest[v1] - rest[v0] from the rest positions, the same single subtraction
+ * StoreRigidityInformation makes.  slice_ptr is int32[ceil(nv/32)+1];
  * mo_sell_plan fills it asynchronously, the record count ending up in
  * slice_ptr[ceil(nv/32)] (read it before sizing the records for
  * mo_sell_fill). */
 int mo_sell_plan(const void* csr, int64_t nv, int64_t nh, int32_t* slice_ptr, void* stream);
-int mo_sell_fill(const void* csr, int64_t nv, int64_t nh, const float* off,
-                 const int32_t* slice_ptr, float* records, void* stream);
+int mo_sell_fill(const void* csr, int64_t nv, int64_t nh, const int32_t* slice_ptr, int32_t* records,
+                 void* stream);
 
 /* ------------------------------------------------------------------------
  * Adam.  Replaces torch.optim.Adam([V], lr) in the reference's loops
@@ -196,7 +199,8 @@ int mo_adam_step(float* P, const float* G, float* M, float* Vsq, int64_t n, floa
 typedef struct MoPair {
     const float* grid;      /* layout-specific grid */
     const int32_t* slice_ptr;
-    const float* sell;      /* float4 records */
+    const int32_t* sell;    /* sliced-ELL records (mo_sell_fill) */
+    const float* rest;      /* float4 [nv] rest positions the offsets are taken from */
     float* pos0;            /* float4 [nv] positions, even steps read pos0 */
     float* pos1;            /* float4 [nv] positions, odd steps read pos1 */
     float* adam_m;          /* float [nv*3] */
@@ -222,9 +226,11 @@ typedef struct MoTile {
 } MoTile;
 
 /* One step (launch_index = 0.. within a group of launches; step t =
- * t0 + launch_index + 1).  tile_loss[launch_index*max_tiles + tile] gets the
- * tile's loss partial.  ntiles is read from device memory.  grid_ctas <= 0
- * picks a persistent grid of resident CTAs. */
+ * t0 + launch_index + 1).  tile_loss[(launch_index*max_tiles + tile)*8 + w]
+ * gets the loss partial of warp w of the tile (MO_TILE_WARPS floats per
+ * tile).  ntiles is read from device memory.  grid_ctas <= 0 picks a
+ * persistent grid of resident CTAs. */
+#define MO_TILE_WARPS 8
 int mo_fused_step(const MoPair* pairs, const MoTile* tiles, const int32_t* ntiles, int max_tiles,
                   int launch_index, float* tile_loss, int grid_ctas, void* stream);
 /* pair_loss[k*npairs + p] (double) = sum, in tile order, of the tile

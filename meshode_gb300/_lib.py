@@ -15,6 +15,7 @@ MO_OK, MO_ERR_INVALID, MO_ERR_CUDA, MO_ERR_SCRATCH, MO_ERR_DEVICE = 0, 1, 2, 3, 
 MO_LAYOUT_LINEAR, MO_LAYOUT_CELL = 0, 1
 MO_DF_AUTO, MO_DF_BRUTE, MO_DF_LBVH = 0, 1, 2
 MO_EDGES_FACES, MO_EDGES_LIST = 0, 1
+MO_TILE_WARPS = 8
 
 _P = ctypes.c_void_p
 _I = ctypes.c_int
@@ -25,7 +26,7 @@ _SZ = ctypes.c_size_t
 
 class MoPair(ctypes.Structure):
     _fields_ = [
-        ("grid", _P), ("slice_ptr", _P), ("sell", _P), ("pos0", _P), ("pos1", _P),
+        ("grid", _P), ("slice_ptr", _P), ("sell", _P), ("rest", _P), ("pos0", _P), ("pos1", _P),
         ("adam_m", _P), ("adam_v", _P), ("adam_tab", _P), ("grad_dbg", _P),
         ("N", ctypes.c_int32), ("layout", ctypes.c_int32), ("nv", ctypes.c_int32), ("nslices", ctypes.c_int32),
         ("w_edge", _F), ("mask_thresh", _F), ("use_mask", ctypes.c_int32), ("grad_scale", _F),
@@ -65,7 +66,7 @@ _SIGS = {
     "mo_edge_csr_build": (_I, [_P, _I64, _I, _I64, _P, _SZ, _P, _P]),
     "mo_edge_backward": (_I, [_P, _I64, _P, _I64, _P, _P, _P]),
     "mo_sell_plan": (_I, [_P, _I64, _I64, _P, _P]),
-    "mo_sell_fill": (_I, [_P, _I64, _I64, _P, _P, _P, _P]),
+    "mo_sell_fill": (_I, [_P, _I64, _I64, _P, _P, _P]),
     "mo_adam_step": (_I, [_P, _P, _P, _P, _I64, _F, _F, _F, _F, _F, _F, _P]),
     "mo_fused_step": (_I, [_P, _P, _P, _I, _I, _P, _I, _P]),
     "mo_pair_loss": (_I, [_P, _I, _I, _I, _P, _P, _P]),

@@ -80,94 +80,123 @@ __global__ void k_normalize_copy(const float* __restrict__ V, int64_t n, const d
 }
 
 // ---------------------------------------------------------------------------
-// Triangle records: 4 float4 = {a, inv|ab|^2}, {b, inv|bc|^2}, {c, inv|ca|^2},
-// {unit normal, nondegenerate flag}.
+// Triangle records, 5 float4 (80 B), in a per-triangle 2D frame so a query
+// costs a projection and three 2D segment distances:
+//   r0 = (a, bx)  r1 = (ex, cx)  r2 = (ey, cy)  r3 = (n, 1)
+//   r4 = (1/bx, 1/|ac|^2, 1/|bc|^2, cx - bx)
+// with ex = ab/|ab|, n the unit normal, ey = n x ex, and the triangle at
+// A=(0,0), B=(bx,0), C=(cx,cy), cy > 0 in (ex, ey).  A degenerate triangle
+// (zero area or zero-length ab) keeps its vertices instead and is measured
+// by its three segments:
+//   r0 = (a, 0)  r1 = (b, 0)  r2 = (c, 0)  r3 = (0, 0, 0, 0)
+//   r4 = (1/|ab|^2, 1/|bc|^2, 1/|ca|^2, 0)   (0 for a zero-length segment)
 // ---------------------------------------------------------------------------
 struct Tri {
-    float4 a, b, c, n;
+    float4 r0, r1, r2, r3, r4;
 };
+constexpr int TRI_F4 = 5;
 
 __device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz) {
     return ax * bx + ay * by + az * bz;
 }
 
-__device__ Tri make_tri(const float* __restrict__ Vn, int i0, int i1, int i2) {
+__device__ Tri make_tri(const float* __restrict__ Vn, int i0, int i1, int i2, float4* lo, float4* hi) {
     const float ax = Vn[3 * (int64_t)i0], ay = Vn[3 * (int64_t)i0 + 1], az = Vn[3 * (int64_t)i0 + 2];
     const float bx = Vn[3 * (int64_t)i1], by = Vn[3 * (int64_t)i1 + 1], bz = Vn[3 * (int64_t)i1 + 2];
     const float cx = Vn[3 * (int64_t)i2], cy = Vn[3 * (int64_t)i2 + 1], cz = Vn[3 * (int64_t)i2 + 2];
+    *lo = make_float4(fminf(fminf(ax, bx), cx), fminf(fminf(ay, by), cy), fminf(fminf(az, bz), cz), 0.f);
+    *hi = make_float4(fmaxf(fmaxf(ax, bx), cx), fmaxf(fmaxf(ay, by), cy), fmaxf(fmaxf(az, bz), cz), 0.f);
     const float abx = bx - ax, aby = by - ay, abz = bz - az;
-    const float bcx = cx - bx, bcy = cy - by, bcz = cz - bz;
-    const float cax = ax - cx, cay = ay - cy, caz = az - cz;
-    const float lab = dot3(abx, aby, abz, abx, aby, abz);
-    const float lbc = dot3(bcx, bcy, bcz, bcx, bcy, bcz);
-    const float lca = dot3(cax, cay, caz, cax, cay, caz);
-    // normal = ab x ac
     const float acx = cx - ax, acy = cy - ay, acz = cz - az;
+    const float lab = dot3(abx, aby, abz, abx, aby, abz);
     float nx = aby * acz - abz * acy, ny = abz * acx - abx * acz, nz = abx * acy - aby * acx;
     const float nn = dot3(nx, ny, nz, nx, ny, nz);
-    float flag = 0.f;
-    if (nn > 0.f && isfinite(nn)) {
-        const float inv = rsqrtf(nn);
-        nx *= inv; ny *= inv; nz *= inv;
-        flag = 1.f;
-    } else {
-        nx = ny = nz = 0.f;
-    }
     Tri t;
-    t.a = make_float4(ax, ay, az, lab > 0.f ? 1.0f / lab : 0.f);
-    t.b = make_float4(bx, by, bz, lbc > 0.f ? 1.0f / lbc : 0.f);
-    t.c = make_float4(cx, cy, cz, lca > 0.f ? 1.0f / lca : 0.f);
-    t.n = make_float4(nx, ny, nz, flag);
+    if (nn > 0.f && isfinite(nn) && lab > 0.f) {
+        const float inn = rsqrtf(nn);
+        nx *= inn; ny *= inn; nz *= inn;
+        const float len = sqrtf(lab), il = 1.0f / len;
+        const float ex = abx * il, ey = aby * il, ez = abz * il;
+        const float yx = ny * ez - nz * ey, yy = nz * ex - nx * ez, yz = nx * ey - ny * ex;  // n x ex
+        const float c2x = dot3(acx, acy, acz, ex, ey, ez), c2y = dot3(acx, acy, acz, yx, yy, yz);
+        const float ebx = c2x - len;
+        const float lac = c2x * c2x + c2y * c2y, lbc = ebx * ebx + c2y * c2y;
+        t.r0 = make_float4(ax, ay, az, len);
+        t.r1 = make_float4(ex, ey, ez, c2x);
+        t.r2 = make_float4(yx, yy, yz, c2y);
+        t.r3 = make_float4(nx, ny, nz, 1.f);
+        t.r4 = make_float4(1.0f / len, lac > 0.f ? 1.0f / lac : 0.f, lbc > 0.f ? 1.0f / lbc : 0.f, ebx);
+    } else {
+        const float bcx = cx - bx, bcy = cy - by, bcz = cz - bz;
+        const float lbc = dot3(bcx, bcy, bcz, bcx, bcy, bcz);
+        const float lca = dot3(acx, acy, acz, acx, acy, acz);
+        t.r0 = make_float4(ax, ay, az, 0.f);
+        t.r1 = make_float4(bx, by, bz, 0.f);
+        t.r2 = make_float4(cx, cy, cz, 0.f);
+        t.r3 = make_float4(0.f, 0.f, 0.f, 0.f);
+        t.r4 = make_float4(lab > 0.f ? 1.0f / lab : 0.f, lbc > 0.f ? 1.0f / lbc : 0.f, lca > 0.f ? 1.0f / lca : 0.f,
+                           0.f);
+    }
     return t;
 }
 
-__device__ __forceinline__ float seg_d2(float px, float py, float pz, float4 a, float ex, float ey, float ez) {
+__device__ __forceinline__ float seg3_d2(float px, float py, float pz, float4 a, float4 b, float inv_l2) {
+    const float ex = b.x - a.x, ey = b.y - a.y, ez = b.z - a.z;
     const float apx = px - a.x, apy = py - a.y, apz = pz - a.z;
-    float t = dot3(apx, apy, apz, ex, ey, ez) * a.w;
+    float t = dot3(apx, apy, apz, ex, ey, ez) * inv_l2;
     t = fminf(fmaxf(t, 0.f), 1.f);
     const float qx = apx - t * ex, qy = apy - t * ey, qz = apz - t * ez;
     return dot3(qx, qy, qz, qx, qy, qz);
 }
 
-// Squared distance from p to the triangle: the interior plane distance when
-// the projection falls inside, else the nearest of the three edge segments.
-__device__ __forceinline__ float tri_d2(float px, float py, float pz, const Tri& T) {
-    const float abx = T.b.x - T.a.x, aby = T.b.y - T.a.y, abz = T.b.z - T.a.z;
-    const float bcx = T.c.x - T.b.x, bcy = T.c.y - T.b.y, bcz = T.c.z - T.b.z;
-    const float cax = T.a.x - T.c.x, cay = T.a.y - T.c.y, caz = T.a.z - T.c.z;
-    float d = seg_d2(px, py, pz, T.a, abx, aby, abz);
-    d = fminf(d, seg_d2(px, py, pz, T.b, bcx, bcy, bcz));
-    d = fminf(d, seg_d2(px, py, pz, T.c, cax, cay, caz));
-    if (T.n.w != 0.f) {
-        const float apx = px - T.a.x, apy = py - T.a.y, apz = pz - T.a.z;
-        const float bpx = px - T.b.x, bpy = py - T.b.y, bpz = pz - T.b.z;
-        const float cpx = px - T.c.x, cpy = py - T.c.y, cpz = pz - T.c.z;
-        // (edge x (p - edge start)) . n >= 0 on all three edges <=> inside
-        const float s0 = dot3(aby * apz - abz * apy, abz * apx - abx * apz, abx * apy - aby * apx, T.n.x, T.n.y, T.n.z);
-        const float s1 = dot3(bcy * bpz - bcz * bpy, bcz * bpx - bcx * bpz, bcx * bpy - bcy * bpx, T.n.x, T.n.y, T.n.z);
-        const float s2 = dot3(cay * cpz - caz * cpy, caz * cpx - cax * cpz, cax * cpy - cay * cpx, T.n.x, T.n.y, T.n.z);
-        if (s0 >= 0.f && s1 >= 0.f && s2 >= 0.f) {
-            const float h = dot3(apx, apy, apz, T.n.x, T.n.y, T.n.z);
-            d = fminf(d, h * h);
-        }
+// Squared distance from p to the triangle.  `cut` is this lane's current
+// best: when no lane of the (converged) warp can beat its best because the
+// plane distance alone is too large, the in-plane part is skipped and
+// FLT_MAX returned.  The record is warp-uniform, so both branches are too.
+__device__ __forceinline__ float tri_d2(float px, float py, float pz, const Tri& T, float cut) {
+    if (T.r3.w != 0.f) {
+        const float qx = px - T.r0.x, qy = py - T.r0.y, qz = pz - T.r0.z;
+        const float h = dot3(qx, qy, qz, T.r3.x, T.r3.y, T.r3.z);
+        const float h2 = h * h;
+        if (!__any_sync(0xffffffffu, h2 < cut)) return FLT_MAX;
+        const float x = dot3(qx, qy, qz, T.r1.x, T.r1.y, T.r1.z);
+        const float y = dot3(qx, qy, qz, T.r2.x, T.r2.y, T.r2.z);
+        const float bx = T.r0.w, cx = T.r1.w, cy = T.r2.w, ebx = T.r4.w;
+        // A-B along the x axis
+        float t = fminf(fmaxf(x * T.r4.x, 0.f), 1.f);
+        float dx = x - t * bx;
+        float d = dx * dx + y * y;
+        // A-C
+        t = fminf(fmaxf((x * cx + y * cy) * T.r4.y, 0.f), 1.f);
+        dx = x - t * cx;
+        float dy = y - t * cy;
+        d = fminf(d, dx * dx + dy * dy);
+        // B-C
+        const float xb = x - bx;
+        t = fminf(fmaxf((xb * ebx + y * cy) * T.r4.z, 0.f), 1.f);
+        dx = xb - t * ebx;
+        dy = y - t * cy;
+        d = fminf(d, dx * dx + dy * dy);
+        // inside: left of A->B, B->C and C->A (counter-clockwise in the frame)
+        const bool inside = (y >= 0.f) && (ebx * y - cy * xb >= 0.f) && (cy * x - cx * y >= 0.f);
+        return h2 + (inside ? 0.f : d);
     }
+    float d = seg3_d2(px, py, pz, T.r0, T.r1, T.r4.x);
+    d = fminf(d, seg3_d2(px, py, pz, T.r1, T.r2, T.r4.y));
+    d = fminf(d, seg3_d2(px, py, pz, T.r2, T.r0, T.r4.z));
     return d;
 }
 
 __device__ __forceinline__ Tri load_tri(const float4* __restrict__ tris, int i) {
+    const float4* p = tris + TRI_F4 * (int64_t)i;
     Tri t;
-    t.a = __ldg(tris + 4 * (int64_t)i);
-    t.b = __ldg(tris + 4 * (int64_t)i + 1);
-    t.c = __ldg(tris + 4 * (int64_t)i + 2);
-    t.n = __ldg(tris + 4 * (int64_t)i + 3);
+    t.r0 = __ldg(p); t.r1 = __ldg(p + 1); t.r2 = __ldg(p + 2); t.r3 = __ldg(p + 3); t.r4 = __ldg(p + 4);
     return t;
 }
 
 __device__ __forceinline__ void store_tri(float4* __restrict__ tris, int i, const Tri& t) {
-    tris[4 * (int64_t)i] = t.a;
-    tris[4 * (int64_t)i + 1] = t.b;
-    tris[4 * (int64_t)i + 2] = t.c;
-    tris[4 * (int64_t)i + 3] = t.n;
+    float4* p = tris + TRI_F4 * (int64_t)i;
+    p[0] = t.r0; p[1] = t.r1; p[2] = t.r2; p[3] = t.r3; p[4] = t.r4;
 }
 
 // ---------------------------------------------------------------------------
@@ -218,13 +247,19 @@ __global__ void k_check_faces(const int32_t* __restrict__ F, int64_t nf, int64_t
 
 // Sorted triangle records (leaf order) from the sorted ids.
 __global__ void k_tri_records(const float* __restrict__ Vn, const int32_t* __restrict__ F, int64_t nf,
-                              int64_t nv, const int* __restrict__ order, float4* __restrict__ tris) {
+                              int64_t nv, const int* __restrict__ order, float4* __restrict__ tris,
+                              float4* __restrict__ boxes) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nf) return;
     const int64_t f = order ? order[i] : i;
     int i0 = F[3 * f], i1 = F[3 * f + 1], i2 = F[3 * f + 2];
     if (i0 < 0 || i1 < 0 || i2 < 0 || i0 >= nv || i1 >= nv || i2 >= nv) i0 = i1 = i2 = 0;  // flagged earlier
-    store_tri(tris, (int)i, make_tri(Vn, i0, i1, i2));
+    float4 lo, hi;
+    store_tri(tris, (int)i, make_tri(Vn, i0, i1, i2, &lo, &hi));
+    if (boxes) {
+        boxes[2 * i] = lo;
+        boxes[2 * i + 1] = hi;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -279,15 +314,13 @@ __device__ __forceinline__ void write_child_box(float4* nodes, int p, int side, 
 }
 
 // Bottom-up refit: the second thread to reach a node merges its children.
-__global__ void k_refit(const float4* __restrict__ tris, int n, float4* nodes, const int* __restrict__ parent,
+__global__ void k_refit(const float4* __restrict__ boxes, int n, float4* nodes, const int* __restrict__ parent,
                         int* flags, float* rootbox, int* status) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
-    const Tri t = load_tri(tris, j);
-    float lo[3] = {fminf(fminf(t.a.x, t.b.x), t.c.x), fminf(fminf(t.a.y, t.b.y), t.c.y),
-                   fminf(fminf(t.a.z, t.b.z), t.c.z)};
-    float hi[3] = {fmaxf(fmaxf(t.a.x, t.b.x), t.c.x), fmaxf(fmaxf(t.a.y, t.b.y), t.c.y),
-                   fmaxf(fmaxf(t.a.z, t.b.z), t.c.z)};
+    const float4 blo = boxes[2 * (int64_t)j], bhi = boxes[2 * (int64_t)j + 1];
+    float lo[3] = {blo.x, blo.y, blo.z};
+    float hi[3] = {bhi.x, bhi.y, bhi.z};
     int slot = (n - 1) + j;
     // A Karras tree over distinct (code, index) keys is at most 64 levels
     // deep; the bound only guards against a corrupted parent array.
@@ -347,7 +380,8 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) k_df_lbvh(const float4* __res
     float best = valid ? FLT_MAX : -1.0f;
     const unsigned FULL = 0xffffffffu;
     if (ntri == 1) {
-        best = valid ? tri_d2(px, py, pz, load_tri(tris, 0)) : best;
+        const float t = tri_d2(px, py, pz, load_tri(tris, 0), best);
+        if (valid) best = t;
     } else {
         int sp = 0;
         int node = 0;
@@ -366,12 +400,12 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) k_df_lbvh(const float4* __res
             bool wl = __any_sync(FULL, dl < best);
             bool wr = __any_sync(FULL, dr < best);
             if (wl && L < 0) {
-                const float t = tri_d2(px, py, pz, load_tri(tris, ~L));
+                const float t = tri_d2(px, py, pz, load_tri(tris, ~L), best);
                 if (valid) best = fminf(best, t);
                 wl = false;
             }
             if (wr && R < 0) {
-                const float t = tri_d2(px, py, pz, load_tri(tris, ~R));
+                const float t = tri_d2(px, py, pz, load_tri(tris, ~R), best);
                 if (valid) best = fminf(best, t);
                 wr = false;
             }
@@ -406,7 +440,7 @@ constexpr int BF_THREADS = 256, BF_CHUNK = 128;
 
 __global__ void __launch_bounds__(BF_THREADS) k_df_brute(const float4* __restrict__ tris, int ntri, int N,
                                                          float* __restrict__ grid) {
-    __shared__ float4 sh[BF_CHUNK * 4];
+    __shared__ float4 sh[BF_CHUNK * TRI_F4];
     const int64_t v = (int64_t)blockIdx.x * BF_THREADS + threadIdx.x;
     const int64_t nvox = (int64_t)N * N * N;
     const bool valid = v < nvox;
@@ -417,12 +451,13 @@ __global__ void __launch_bounds__(BF_THREADS) k_df_brute(const float4* __restric
     for (int base = 0; base < ntri; base += BF_CHUNK) {
         const int cnt = min(BF_CHUNK, ntri - base);
         __syncthreads();
-        for (int k = threadIdx.x; k < cnt * 4; k += BF_THREADS) sh[k] = tris[4 * (int64_t)base + k];
+        for (int k = threadIdx.x; k < cnt * TRI_F4; k += BF_THREADS) sh[k] = tris[TRI_F4 * (int64_t)base + k];
         __syncthreads();
         for (int t = 0; t < cnt; ++t) {
             Tri T;
-            T.a = sh[4 * t]; T.b = sh[4 * t + 1]; T.c = sh[4 * t + 2]; T.n = sh[4 * t + 3];
-            best = fminf(best, tri_d2(px, py, pz, T));
+            T.r0 = sh[TRI_F4 * t]; T.r1 = sh[TRI_F4 * t + 1]; T.r2 = sh[TRI_F4 * t + 2];
+            T.r3 = sh[TRI_F4 * t + 3]; T.r4 = sh[TRI_F4 * t + 4];
+            best = fminf(best, tri_d2(px, py, pz, T, valid ? best : -1.0f));
         }
     }
     if (valid) grid[v] = __fsqrt_rn(best);
@@ -439,6 +474,7 @@ struct BuildScratch {
     int* ids_a;
     int* ids_b;
     float4* nodes;
+    float4* boxes;
     int* parent;
     int* flags;
     int* hist;
@@ -460,13 +496,14 @@ static BuildScratch plan_scratch(char* base, int64_t nv, int64_t nf, int method)
     s.status = reinterpret_cast<int*>(take(sizeof(int) * 4));
     s.rootbox = reinterpret_cast<float*>(take(sizeof(float) * 8));
     s.Vn = reinterpret_cast<float*>(take(sizeof(float) * 3 * (size_t)nv));
-    s.tris = reinterpret_cast<float4*>(take(sizeof(float4) * 4 * (size_t)nf));
+    s.tris = reinterpret_cast<float4*>(take(sizeof(float4) * TRI_F4 * (size_t)nf));
     if (method == MO_DF_LBVH) {
         s.codes_a = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * (size_t)nf));
         s.codes_b = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * (size_t)nf));
         s.ids_a = reinterpret_cast<int*>(take(sizeof(int) * (size_t)nf));
         s.ids_b = reinterpret_cast<int*>(take(sizeof(int) * (size_t)nf));
         s.nodes = reinterpret_cast<float4*>(take(sizeof(float4) * 4 * (size_t)(nf > 1 ? nf - 1 : 1)));
+        s.boxes = reinterpret_cast<float4*>(take(sizeof(float4) * 2 * (size_t)nf));
         s.parent = reinterpret_cast<int*>(take(sizeof(int) * (size_t)(2 * nf)));
         s.flags = reinterpret_cast<int*>(take(sizeof(int) * (size_t)nf));
         s.hist = reinterpret_cast<int*>(take(sizeof(int) * radix_hist_ints((int)nf)));
@@ -474,6 +511,7 @@ static BuildScratch plan_scratch(char* base, int64_t nv, int64_t nf, int method)
         s.codes_a = s.codes_b = nullptr;
         s.ids_a = s.ids_b = nullptr;
         s.nodes = nullptr;
+        s.boxes = nullptr;
         s.parent = s.flags = s.hist = nullptr;
     }
     s.bytes = o;
@@ -561,17 +599,17 @@ extern "C" int mo_df_build(const float* V, int64_t nv, const int32_t* F, int64_t
         k_normalize_copy<<<ceil_div(3 * nv, 256), 256, 0, s>>>(V, nv, params4, S.Vn); ::mo::note_launch();
         if (method == MO_DF_BRUTE) {
             k_check_faces<<<ceil_div(nf, 256), 256, 0, s>>>(F, nf, nv, st); ::mo::note_launch();
-            k_tri_records<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, nullptr, S.tris); ::mo::note_launch();
+            k_tri_records<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, nullptr, S.tris, nullptr); ::mo::note_launch();
             const int64_t nvox = (int64_t)N * N * N;
             k_df_brute<<<ceil_div(nvox, BF_THREADS), BF_THREADS, 0, s>>>(S.tris, (int)nf, N, grid_out); ::mo::note_launch();
         } else {
             k_morton<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.codes_a, S.ids_a, st); ::mo::note_launch();
             e = radix_sort_pairs(S.codes_a, S.ids_a, S.codes_b, S.ids_b, (int)nf, 30, S.hist, s);
             if (e != cudaSuccess) { fail(e, "radix_sort_pairs"); break; }
-            k_tri_records<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.ids_a, S.tris); ::mo::note_launch();
+            k_tri_records<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.ids_a, S.tris, S.boxes); ::mo::note_launch();
             if (nf > 1) {
                 k_karras<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.codes_a, (int)nf, S.nodes, S.parent, S.flags); ::mo::note_launch();
-                k_refit<<<ceil_div(nf, 256), 256, 0, s>>>(S.tris, (int)nf, S.nodes, S.parent, S.flags, S.rootbox, st); ::mo::note_launch();
+                k_refit<<<ceil_div(nf, 256), 256, 0, s>>>(S.boxes, (int)nf, S.nodes, S.parent, S.flags, S.rootbox, st); ::mo::note_launch();
             }
             const int64_t bricks = (int64_t)((N + 3) / 4) * ((N + 3) / 4) * ((N + 1) / 2);
             k_df_lbvh<<<ceil_div(bricks, TRAV_WARPS), TRAV_WARPS * 32, 0, s>>>(S.nodes, S.tris, (int)nf, N,
@@ -619,10 +657,10 @@ extern "C" int mo_lbvh_build(const float* V, int64_t nv, const int32_t* F, int64
         e = radix_sort_pairs(S.codes_a, S.ids_a, S.codes_b, S.ids_b, (int)nf, 30, S.hist, s);
     }
     if (e == cudaSuccess) {
-        k_tri_records<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.ids_a, S.tris); ::mo::note_launch();
+        k_tri_records<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.ids_a, S.tris, S.boxes); ::mo::note_launch();
         if (nf > 1) {
             k_karras<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.codes_a, (int)nf, S.nodes, S.parent, S.flags); ::mo::note_launch();
-            k_refit<<<ceil_div(nf, 256), 256, 0, s>>>(S.tris, (int)nf, S.nodes, S.parent, S.flags, S.rootbox,
+            k_refit<<<ceil_div(nf, 256), 256, 0, s>>>(S.boxes, (int)nf, S.nodes, S.parent, S.flags, S.rootbox,
                                                       S.status); ::mo::note_launch();
         }
         e = cudaGetLastError();

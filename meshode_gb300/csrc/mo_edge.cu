@@ -168,8 +168,7 @@ __global__ void k_sell_width(int64_t nv, int64_t nslices, const int* __restrict_
 
 __global__ void k_sell_fill(int64_t nv, int64_t nslices, const int* __restrict__ row_ptr,
                             const int* __restrict__ key, const int* __restrict__ other,
-                            const float* __restrict__ off, const int* __restrict__ slice_ptr,
-                            float4* __restrict__ rec) {
+                            const int* __restrict__ slice_ptr, int* __restrict__ rec) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t s = t >> 5;
     const int lane = threadIdx.x & 31;
@@ -179,18 +178,8 @@ __global__ void k_sell_fill(int64_t nv, int64_t nslices, const int* __restrict__
     const int w = (slice_ptr[s + 1] - base) >> 5;
     const int b = v < nv ? row_ptr[v] : 0;
     const int deg = v < nv ? row_ptr[v + 1] - b : 0;
-    for (int k = 0; k < w; ++k) {
-        float4 r;
-        if (k < deg) {
-            const int kk = key[b + k];
-            const int64_t h = kk >> 1;
-            const int code = other[b + k] | ((kk & 1) << 31);
-            r = make_float4(__int_as_float(code), off[3 * h], off[3 * h + 1], off[3 * h + 2]);
-        } else {
-            r = make_float4(__int_as_float(-1), 0.f, 0.f, 0.f);
-        }
-        rec[base + (int64_t)k * 32 + lane] = r;
-    }
+    for (int k = 0; k < w; ++k)
+        rec[base + (int64_t)k * 32 + lane] = (k < deg) ? (other[b + k] | ((key[b + k] & 1) << 31)) : -1;
 }
 
 }  // namespace mo
@@ -311,16 +300,15 @@ extern "C" int mo_sell_plan(const void* csr, int64_t nv, int64_t nh, int32_t* sl
     return MO_OK;
 }
 
-extern "C" int mo_sell_fill(const void* csr, int64_t nv, int64_t nh, const float* off, const int32_t* slice_ptr,
-                            float* records, void* stream) {
+extern "C" int mo_sell_fill(const void* csr, int64_t nv, int64_t nh, const int32_t* slice_ptr, int32_t* records,
+                            void* stream) {
     MO_CHECK_ARG(nv >= 0 && nh >= 0, "negative size");
     if (nv == 0) return MO_OK;
-    MO_CHECK_ARG(csr && slice_ptr && records && (nh == 0 || off), "null pointer");
-    MO_CHECK_ARG(aligned(records, 16), "records must be 16-byte aligned");
+    MO_CHECK_ARG(csr && slice_ptr && records, "null pointer");
     const int64_t nslices = (nv + 31) / 32;
     CsrView c = csr_view(const_cast<void*>(csr), nv, nh);
-    k_sell_fill<<<ceil_div(nslices * 32, 256), 256, 0, as_stream(stream)>>>(
-        nv, nslices, c.row_ptr, c.key, c.other, off, slice_ptr, reinterpret_cast<float4*>(records)); ::mo::note_launch();
+    k_sell_fill<<<ceil_div(nslices * 32, 256), 256, 0, as_stream(stream)>>>(nv, nslices, c.row_ptr, c.key, c.other,
+                                                                           slice_ptr, records); ::mo::note_launch();
     MO_LAUNCH_CHECK("k_sell_fill");
     return MO_OK;
 }

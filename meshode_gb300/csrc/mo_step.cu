@@ -33,6 +33,9 @@ __global__ void __launch_bounds__(256) k_adam(float* __restrict__ P, const float
 }
 
 constexpr int STEP_THREADS = 256;  // 8 warps = up to 8 slices of 32 vertices
+constexpr int TILE_WARPS = STEP_THREADS / 32;
+static_assert(TILE_WARPS == MO_TILE_WARPS, "tile warps");
+constexpr int REC_UNROLL = 2;      // record rows fetched ahead of their neighbour gathers
 
 template <int LAYOUT>
 __device__ __forceinline__ DFJet df_eval_layout(const float* grid, int N, float Nf, float Cf, float x, float y,
@@ -40,97 +43,116 @@ __device__ __forceinline__ DFJet df_eval_layout(const float* grid, int N, float 
     return df_eval<LAYOUT, true>(grid, N, Nf, Cf, x, y, z);
 }
 
+// Every warp owns one 32-vertex slice of a tile and never waits for the
+// other warps of its block.
 __global__ void __launch_bounds__(STEP_THREADS) k_fused_step(const MoPair* __restrict__ pairs,
                                                              const MoTile* __restrict__ tiles,
                                                              const int* __restrict__ ntiles_p, int max_tiles,
                                                              int k, float* __restrict__ tile_loss) {
-    __shared__ float red[STEP_THREADS / 32];
     const int ntiles = min(*ntiles_p, max_tiles);
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const MoTile T = tiles[tile];
         const MoPair& P = pairs[T.pair];
+        float* out = tile_loss + ((int64_t)k * max_tiles + tile) * TILE_WARPS + w;
         const int t = P.t0 + k + 1;
-        if (t > P.t_end) {  // uniform across the block
-            if (threadIdx.x == 0) tile_loss[(int64_t)k * max_tiles + tile] = 0.f;
+        if (t > P.t_end || w >= T.nslices) {  // warp-uniform
+            if (lane == 0) *out = 0.f;
             continue;
         }
-        float part = 0.f;
-        if (w < T.nslices) {
-            const int slice = T.slice0 + w;
-            const int nv = P.nv;
-            const int i = slice * 32 + lane;
-            const bool valid = i < nv;
-            const float4* __restrict__ Vin = reinterpret_cast<const float4*>((t & 1) ? P.pos0 : P.pos1);
-            float4* __restrict__ Vout = reinterpret_cast<float4*>((t & 1) ? P.pos1 : P.pos0);
-            const float4 p = valid ? Vin[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-            const int N = P.N;
-            const float Nf = (float)N, Cf = (float)((double)(N - 1) - 1e-3);
-            const DFJet j = (P.layout == MO_LAYOUT_CELL) ? df_eval_layout<MO_LAYOUT_CELL>(P.grid, N, Nf, Cf, p.x, p.y, p.z)
-                                                         : df_eval_layout<MO_LAYOUT_LINEAR>(P.grid, N, Nf, Cf, p.x, p.y, p.z);
-            const float dsq = MUL(j.d, j.d);
-            float gdx = df_grad_component(j.d, j.gx);
-            float gdy = df_grad_component(j.d, j.gy);
-            float gdz = df_grad_component(j.d, j.gz);
-            if (P.use_mask) {
-                const float mk = (MUL(dsq, 0.5f) < P.mask_thresh) ? 1.0f : 0.0f;
-                gdx = MUL(gdx, mk); gdy = MUL(gdy, mk); gdz = MUL(gdz, mk);
+        const int slice = T.slice0 + w;
+        const int nv = P.nv;
+        const int i = slice * 32 + lane;
+        const bool valid = i < nv;
+        const float4* __restrict__ Vin = reinterpret_cast<const float4*>((t & 1) ? P.pos0 : P.pos1);
+        float4* __restrict__ Vout = reinterpret_cast<float4*>((t & 1) ? P.pos1 : P.pos0);
+        const float4* __restrict__ R = reinterpret_cast<const float4*>(P.rest);
+        const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 p = valid ? Vin[i] : zero;
+        const float4 r0 = valid ? __ldg(R + i) : zero;
+        float* __restrict__ Mm = P.adam_m + 3 * (int64_t)i;
+        float* __restrict__ Vv = P.adam_v + 3 * (int64_t)i;
+        float m0 = 0.f, m1 = 0.f, m2 = 0.f, v0 = 0.f, v1 = 0.f, v2 = 0.f;
+        if (valid) {
+            m0 = Mm[0]; m1 = Mm[1]; m2 = Mm[2];
+            v0 = Vv[0]; v1 = Vv[1]; v2 = Vv[2];
+        }
+        const int N = P.N;
+        const float Nf = (float)N, Cf = (float)((double)(N - 1) - 1e-3);
+        const DFJet j = (P.layout == MO_LAYOUT_CELL) ? df_eval_layout<MO_LAYOUT_CELL>(P.grid, N, Nf, Cf, p.x, p.y, p.z)
+                                                     : df_eval_layout<MO_LAYOUT_LINEAR>(P.grid, N, Nf, Cf, p.x, p.y, p.z);
+        const float dsq = MUL(j.d, j.d);
+        float gdx = df_grad_component(j.d, j.gx);
+        float gdy = df_grad_component(j.d, j.gy);
+        float gdz = df_grad_component(j.d, j.gz);
+        if (P.use_mask) {
+            const float mk = (MUL(dsq, 0.5f) < P.mask_thresh) ? 1.0f : 0.0f;
+            gdx = MUL(gdx, mk); gdy = MUL(gdy, mk); gdz = MUL(gdz, mk);
+        }
+        // Edge residuals over this vertex's sliced-ELL column, in the order
+        // of the reference's serial scatter.  Rest offset = rest[v1] - rest[v0].
+        float grx = 0.f, gry = 0.f, grz = 0.f, esq = 0.f;
+        const int rb = P.slice_ptr[slice];
+        const int rows = (P.slice_ptr[slice + 1] - rb) >> 5;
+        const int* __restrict__ rec = P.sell + rb + lane;
+        for (int row = 0; row < rows; row += REC_UNROLL) {
+            int c[REC_UNROLL];
+#pragma unroll
+            for (int u = 0; u < REC_UNROLL; ++u) c[u] = (row + u < rows) ? __ldg(rec + (row + u) * 32) : -1;
+            float4 q[REC_UNROLL], sr[REC_UNROLL];
+#pragma unroll
+            for (int u = 0; u < REC_UNROLL; ++u) {
+                if (c[u] != -1) {
+                    const int o = c[u] & 0x7fffffff;
+                    q[u] = Vin[o];
+                    sr[u] = __ldg(R + o);
+                } else {
+                    q[u] = zero;
+                    sr[u] = zero;
+                }
             }
-            // Edge residuals over this vertex's sliced-ELL column, in the
-            // order of the reference's serial scatter.
-            float grx = 0.f, gry = 0.f, grz = 0.f, esq = 0.f;
-            const int rb = P.slice_ptr[slice], re = P.slice_ptr[slice + 1];
-            const float4* __restrict__ rec = reinterpret_cast<const float4*>(P.sell);
-            for (int r = rb + lane; r < re; r += 32) {
-                const float4 e = __ldg(rec + r);
-                const int code = __float_as_int(e.x);
-                if (code == -1) break;  // padding follows the last real record
-                const float4 q = Vin[code & 0x7fffffff];
-                if (code >= 0) {  // vertex is v0 of the half-edge: g -= v1 - v0 - off
-                    const float rx = SUB(SUB(q.x, p.x), e.y), ry = SUB(SUB(q.y, p.y), e.z), rz = SUB(SUB(q.z, p.z), e.w);
+#pragma unroll
+            for (int u = 0; u < REC_UNROLL; ++u) {
+                if (c[u] == -1) break;  // padding follows the last real record
+                if (c[u] >= 0) {  // vertex is v0 of the half-edge: g -= v1 - v0 - off
+                    const float rx = SUB(SUB(q[u].x, p.x), SUB(sr[u].x, r0.x));
+                    const float ry = SUB(SUB(q[u].y, p.y), SUB(sr[u].y, r0.y));
+                    const float rz = SUB(SUB(q[u].z, p.z), SUB(sr[u].z, r0.z));
                     grx = SUB(grx, rx); gry = SUB(gry, ry); grz = SUB(grz, rz);
                     esq += rx * rx + ry * ry + rz * rz;
                 } else {          // vertex is v1: g += v1 - v0 - off
-                    const float rx = SUB(SUB(p.x, q.x), e.y), ry = SUB(SUB(p.y, q.y), e.z), rz = SUB(SUB(p.z, q.z), e.w);
+                    const float rx = SUB(SUB(p.x, q[u].x), SUB(r0.x, sr[u].x));
+                    const float ry = SUB(SUB(p.y, q[u].y), SUB(r0.y, sr[u].y));
+                    const float rz = SUB(SUB(p.z, q[u].z), SUB(r0.z, sr[u].z));
                     grx = ADD(grx, rx); gry = ADD(gry, ry); grz = ADD(grz, rz);
                 }
             }
-            // grad_h * (gD + gR * w)  (graph_loss_layer.py:42, rigid_loss_layer.py:27)
-            const float we = P.w_edge, gh = P.grad_scale;
-            const float gx = MUL(gh, ADD(gdx, MUL(grx, we)));
-            const float gy = MUL(gh, ADD(gdy, MUL(gry, we)));
-            const float gz = MUL(gh, ADD(gdz, MUL(grz, we)));
-            if (valid) {
-                if (P.grad_dbg) {
-                    P.grad_dbg[3 * (int64_t)i] = gx;
-                    P.grad_dbg[3 * (int64_t)i + 1] = gy;
-                    P.grad_dbg[3 * (int64_t)i + 2] = gz;
-                }
-                const float2 ab = __ldg(reinterpret_cast<const float2*>(P.adam_tab) + (t - 1));
-                float* __restrict__ Mm = P.adam_m + 3 * (int64_t)i;
-                float* __restrict__ Vv = P.adam_v + 3 * (int64_t)i;
-                float px = p.x, py = p.y, pz = p.z;
-                float m0 = Mm[0], m1 = Mm[1], m2 = Mm[2];
-                float v0 = Vv[0], v1 = Vv[1], v2 = Vv[2];
-                adam_elem(px, gx, m0, v0, P.one_minus_b1, P.b2, P.one_minus_b2, P.eps, ab.x, ab.y);
-                adam_elem(py, gy, m1, v1, P.one_minus_b1, P.b2, P.one_minus_b2, P.eps, ab.x, ab.y);
-                adam_elem(pz, gz, m2, v2, P.one_minus_b1, P.b2, P.one_minus_b2, P.eps, ab.x, ab.y);
-                Mm[0] = m0; Mm[1] = m1; Mm[2] = m2;
-                Vv[0] = v0; Vv[1] = v1; Vv[2] = v2;
-                Vout[i] = make_float4(px, py, pz, 0.f);
-                part = 0.5f * dsq + we * (0.5f * esq);
+            if (c[REC_UNROLL - 1] == -1) break;
+        }
+        // grad_h * (gD + gR * w)  (graph_loss_layer.py:42, rigid_loss_layer.py:27)
+        const float we = P.w_edge, gh = P.grad_scale;
+        const float gx = MUL(gh, ADD(gdx, MUL(grx, we)));
+        const float gy = MUL(gh, ADD(gdy, MUL(gry, we)));
+        const float gz = MUL(gh, ADD(gdz, MUL(grz, we)));
+        float part = 0.f;
+        if (valid) {
+            if (P.grad_dbg) {
+                P.grad_dbg[3 * (int64_t)i] = gx;
+                P.grad_dbg[3 * (int64_t)i + 1] = gy;
+                P.grad_dbg[3 * (int64_t)i + 2] = gz;
             }
+            const float2 ab = __ldg(reinterpret_cast<const float2*>(P.adam_tab) + (t - 1));
+            float px = p.x, py = p.y, pz = p.z;
+            adam_elem(px, gx, m0, v0, P.one_minus_b1, P.b2, P.one_minus_b2, P.eps, ab.x, ab.y);
+            adam_elem(py, gy, m1, v1, P.one_minus_b1, P.b2, P.one_minus_b2, P.eps, ab.x, ab.y);
+            adam_elem(pz, gz, m2, v2, P.one_minus_b1, P.b2, P.one_minus_b2, P.eps, ab.x, ab.y);
+            Mm[0] = m0; Mm[1] = m1; Mm[2] = m2;
+            Vv[0] = v0; Vv[1] = v1; Vv[2] = v2;
+            Vout[i] = make_float4(px, py, pz, 0.f);
+            part = 0.5f * dsq + we * (0.5f * esq);
         }
-        // deterministic block reduction of the loss partial
         for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-        if (lane == 0) red[w] = part;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            float s = 0.f;
-            for (int q = 0; q < STEP_THREADS / 32; ++q) s += red[q];
-            tile_loss[(int64_t)k * max_tiles + tile] = s;
-        }
-        __syncthreads();
+        if (lane == 0) *out = part;
     }
 }
 
@@ -141,7 +163,9 @@ __global__ void k_pair_loss(const MoPair* __restrict__ pairs, int npairs, int ma
     const int p = (int)(q % npairs), k = (int)(q / npairs);
     const MoPair& P = pairs[p];
     double s = 0.0;
-    for (int t = P.tile0; t < P.tile0 + P.ntiles; ++t) s += (double)tile_loss[(int64_t)k * max_tiles + t];
+    const float* base = tile_loss + (int64_t)k * max_tiles * TILE_WARPS;
+    for (int64_t t = (int64_t)P.tile0 * TILE_WARPS; t < (int64_t)(P.tile0 + P.ntiles) * TILE_WARPS; ++t)
+        s += (double)base[t];
     out[(int64_t)k * npairs + p] = s;
 }
 

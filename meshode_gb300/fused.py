@@ -46,12 +46,14 @@ def adam_table(tmax, lr, b1, b2, device):
 class Pair:
     """Optimiser state of one deformation pair on the device."""
 
-    def __init__(self, grid, N, layout, V, csr, nh, offsets, steps, lr=1e-3, betas=(0.9, 0.999), eps=1e-8,
+    def __init__(self, grid, N, layout, V, csr, nh, rest, steps, lr=1e-3, betas=(0.9, 0.999), eps=1e-8,
                  w_edge=1.0, mask_thresh=None, grad_scale=1.0, debug_grad=False, stream=None, slice_ptr=None,
                  nrec=None):
-        """V: normalised source vertices, float32 [nv,3] on the device.
-        csr/nh/offsets: the edge CSR buffer, half-edge count and rest offsets.
-        When slice_ptr/nrec are given, the sliced-ELL plan was already made."""
+        """V: normalised source vertices, float32 [nv,3] on the device (the
+        optimiser's start).  csr/nh: the edge CSR buffer and half-edge count.
+        rest: float32 [nv,3] positions the rest offsets were taken from (the V
+        given to StoreRigidityInformation).  When slice_ptr/nrec are given, the
+        sliced-ELL plan was already made."""
         dev = V.device
         s = stream_ptr(stream)
         self.device = dev
@@ -70,6 +72,8 @@ class Pair:
         self.grad_scale = float(grad_scale)
         self.pos = torch.zeros(2, self.nv, 4, dtype=torch.float32, device=dev)
         call("mo_pack_pos", ptr(V), self.nv, ptr(self.pos[0]), s)
+        self.rest = torch.empty(self.nv, 4, dtype=torch.float32, device=dev)
+        call("mo_pack_pos", ptr(rest.contiguous()), self.nv, ptr(self.rest), s)
         self.m = torch.zeros(self.nv * 3, dtype=torch.float32, device=dev)
         self.v = torch.zeros(self.nv * 3, dtype=torch.float32, device=dev)
         if slice_ptr is None:
@@ -78,14 +82,14 @@ class Pair:
             nrec = int(slice_ptr[self.nslices].item())
         self.slice_ptr = slice_ptr
         self.nrec = int(nrec)
-        self.sell = torch.empty(max(self.nrec, 1) * 4, dtype=torch.float32, device=dev)
-        call("mo_sell_fill", ptr(csr), self.nv, nh, ptr(offsets), ptr(self.slice_ptr), ptr(self.sell), s)
+        self.sell = torch.empty(max(self.nrec, 1), dtype=torch.int32, device=dev)
+        call("mo_sell_fill", ptr(csr), self.nv, nh, ptr(self.slice_ptr), ptr(self.sell), s)
         self.grad_dbg = torch.zeros(self.nv * 3, dtype=torch.float32, device=dev) if debug_grad else None
         self.adam_tab = adam_table(max(self.steps, 1), self.lr, self.b1, self.b2, dev)
         self.loss_history = []
 
     def nbytes(self):
-        return (self.pos.numel() + self.m.numel() + self.v.numel() + self.sell.numel()) * 4 + \
+        return (self.pos.numel() + self.rest.numel() + self.m.numel() + self.v.numel() + self.sell.numel()) * 4 + \
             self.slice_ptr.numel() * 4
 
     @property
@@ -101,6 +105,7 @@ class Pair:
         p.grid = self.grid.data_ptr()
         p.slice_ptr = self.slice_ptr.data_ptr()
         p.sell = self.sell.data_ptr()
+        p.rest = self.rest.data_ptr()
         p.pos0 = self.pos[0].data_ptr()
         p.pos1 = self.pos[1].data_ptr()
         p.adam_m = self.m.data_ptr()
@@ -138,7 +143,7 @@ class StepGroupRunner:
         self.pairs_dev = torch.zeros(self.max_pairs * PAIR_BYTES, dtype=torch.uint8, device=device)
         self.tiles_dev = torch.zeros(self.max_tiles * TILE_BYTES, dtype=torch.uint8, device=device)
         self.ntiles_dev = torch.zeros(1, dtype=torch.int32, device=device)
-        self.tile_loss = torch.zeros(self.S * self.max_tiles, dtype=torch.float32, device=device)
+        self.tile_loss = torch.zeros(self.S * self.max_tiles * L.MO_TILE_WARPS, dtype=torch.float32, device=device)
         self.pair_loss = torch.zeros(self.S * self.max_pairs, dtype=torch.float64, device=device)
         nbytes = self.max_pairs * PAIR_BYTES + self.max_tiles * TILE_BYTES + 4
         self._staging = [torch.zeros(nbytes, dtype=torch.uint8).pin_memory() for _ in range(2)]
@@ -236,7 +241,7 @@ def pair_from_template(pid, src_V_norm, steps, lr=1e-3, w_edge=1.0, mask_thresh=
     if st is None:
         raise RuntimeError("template %d has no stored edge information" % int(pid))
     V = src_V_norm.detach().to(p.device).contiguous()
-    return Pair(p.grid, p.N, p.layout, V, st.csr, st.nh, st.offsets, steps, lr=lr, w_edge=w_edge,
+    return Pair(p.grid, p.N, p.layout, V, st.csr, st.nh, st.rest, steps, lr=lr, w_edge=w_edge,
                 mask_thresh=mask_thresh, debug_grad=debug_grad, **kw)
 
 

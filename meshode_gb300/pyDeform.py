@@ -38,6 +38,7 @@ class _EdgeState:
         self.offsets = offsets      # float32 [nh,3] on the device
         self.csr_cache = {}         # key -> (idx_dev, csr buffer)
         self.csr = None             # CSR of the index tensor given at Store time
+        self.rest = None            # the vertices the rest offsets were taken from
 
 
 class DeformParams:
@@ -283,6 +284,9 @@ def _store_edges(tensorV, idx, param_id, kind):
     # validates the indices against the vertex count (raises on a bad index)
     _, state.csr = _csr_for(state, idx, Id, Vd.shape[0], p.device)
     call("mo_edge_offsets", ptr(Vd), Vd.shape[0], ptr(Id), Id.shape[0], kind, ptr(off), s)
+    # a copy: for a contiguous CUDA input Vd aliases the caller's tensor,
+    # which the caller's optimiser then moves
+    state.rest = Vd.clone()
     p.edge = state
 
 

@@ -68,15 +68,15 @@ def estimate_bytes(nv, nf_src, nv_tar, nf_tar, N, layout=L.MO_LAYOUT_CELL):
     grid = lib.mo_grid_bytes(N, layout) + 4 * N ** 3
     scratch = lib.mo_df_build_scratch_bytes(nv_tar, nf_tar, N, L.MO_DF_AUTO)
     meshes = 12 * (nv + nf_src + nv_tar + nf_tar)
-    edges = 12 * nh + lib.mo_edge_csr_bytes(nv, nf_src, L.MO_EDGES_FACES)
-    sell = 16 * (2 * nh + 32 * ((nv + 31) // 32) * 4)
-    state = 32 * nv + 24 * nv + 4 * ((nv + 31) // 32 + 1) + 12 * nv
+    edges = lib.mo_edge_csr_bytes(nv, nf_src, L.MO_EDGES_FACES)
+    sell = 4 * (2 * nh + 32 * ((nv + 31) // 32) * 4)
+    state = 48 * nv + 24 * nv + 4 * ((nv + 31) // 32 + 1) + 12 * nv
     return int(grid + scratch + meshes + edges + sell + state + (1 << 16))
 
 
 class _Job:
     __slots__ = ("req", "bytes", "phase", "ev", "host", "nv", "nh", "Vd", "Fd", "params", "grid", "csr", "off",
-                 "slice_ptr", "status", "pair", "out_dev", "out_host")
+                 "slice_ptr", "status", "pair", "out_dev", "out_host", "stream")
 
     def __init__(self, req, nbytes):
         self.req = req
@@ -89,7 +89,8 @@ class _Job:
 
 class ServingEngine:
     def __init__(self, device=None, hbm_budget_bytes=None, max_pairs=512, max_tiles=None, group_steps=25,
-                 layout=L.MO_LAYOUT_CELL, use_graph=True, max_building=8, results_to_host=True, lr=1e-3):
+                 layout=L.MO_LAYOUT_CELL, use_graph=True, max_building=8, results_to_host=True, lr=1e-3,
+                 build_streams=2):
         L.require_cuda()
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
         free, total = torch.cuda.mem_get_info(self.device)
@@ -100,7 +101,10 @@ class ServingEngine:
             max_tiles = 1 << 17
         self.runner = fused.StepGroupRunner(self.device, self.max_pairs, int(max_tiles), group_steps=group_steps,
                                             use_graph=use_graph)
-        self.build_stream = torch.cuda.Stream(self.device)
+        # builds alternate between side streams so one build's set-up kernels
+        # and tail overlap another's traversal
+        self.build_streams = [torch.cuda.Stream(self.device) for _ in range(max(1, int(build_streams)))]
+        self._next_build = 0
         self.step_stream = torch.cuda.current_stream(self.device)
         self.max_building = int(max_building)
         self.results_to_host = bool(results_to_host)
@@ -123,8 +127,10 @@ class ServingEngine:
         """Copies, DF build, normalisation, edge offsets, CSR, ELL plan."""
         req = job.req
         lib = L.lib()
-        with torch.cuda.stream(self.build_stream):
-            s = stream_ptr(self.build_stream)
+        job.stream = self.build_streams[self._next_build % len(self.build_streams)]
+        self._next_build += 1
+        with torch.cuda.stream(job.stream):
+            s = stream_ptr(job.stream)
             Vd = self._to_dev(req.srcV, copy=True)  # normalised in place below
             Fd = self._to_dev(req.srcF)
             Td = self._to_dev(req.tarV)
@@ -152,8 +158,6 @@ class ServingEngine:
             del Td, TFd
             call("mo_normalize", ptr(Vd), nv, ptr(job.params), 0, s)
             nh = 3 * nf
-            job.off = torch.empty(nh, 3, dtype=torch.float32, device=self.device)
-            call("mo_edge_offsets", ptr(Vd), nv, ptr(Fd), nf, L.MO_EDGES_FACES, ptr(job.off), s)
             cb = lib.mo_edge_csr_bytes(nv, nf, L.MO_EDGES_FACES)
             job.csr = torch.empty((cb + 3) // 4, dtype=torch.int32, device=self.device)
             call("mo_edge_csr_build", ptr(Fd), nf, L.MO_EDGES_FACES, nv, ptr(job.csr), cb, ptr(job.status[1:2]), s)
@@ -165,7 +169,7 @@ class ServingEngine:
             job.host.copy_(job.status, non_blocking=True)
             job.Vd, job.Fd, job.nv, job.nh = Vd, Fd, nv, nh
             job.ev = torch.cuda.Event()
-            job.ev.record(self.build_stream)
+            job.ev.record(job.stream)
         job.phase = 1
 
     def _phase_b(self, job):
@@ -175,15 +179,17 @@ class ServingEngine:
             job.req.error = "invalid mesh (DF status %d, edge status %d)" % (st[0], st[1])
             return False
         req = job.req
-        with torch.cuda.stream(self.build_stream):
-            job.pair = fused.Pair(job.grid, req.N, self.layout, job.Vd, job.csr, job.nh, job.off, req.steps,
-                                  lr=req.lr, w_edge=req.w_edge, stream=self.build_stream, slice_ptr=job.slice_ptr,
+        with torch.cuda.stream(job.stream):
+            # the rest offsets are taken from the normalised source itself
+            job.pair = fused.Pair(job.grid, req.N, self.layout, job.Vd, job.csr, job.nh, job.Vd, req.steps,
+                                  lr=req.lr, w_edge=req.w_edge, stream=job.stream, slice_ptr=job.slice_ptr,
                                   nrec=st[2])
             job.csr = job.off = job.Fd = job.Vd = None
-            for t in (job.grid, job.pair.pos, job.pair.m, job.pair.v, job.pair.sell, job.pair.slice_ptr, job.params):
+            for t in (job.grid, job.pair.pos, job.pair.rest, job.pair.m, job.pair.v, job.pair.sell,
+                      job.pair.slice_ptr, job.params):
                 t.record_stream(self.step_stream)
             job.ev = torch.cuda.Event()
-            job.ev.record(self.build_stream)
+            job.ev.record(job.stream)
         job.phase = 2
         return True
 
