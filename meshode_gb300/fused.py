@@ -21,6 +21,10 @@ from ._lib import call, ptr, stream_ptr
 PAIR_BYTES = ctypes.sizeof(L.MoPair)
 TILE_BYTES = ctypes.sizeof(L.MoTile)
 SLICES_PER_TILE = 8
+# int32 word offsets of the per-group fields inside a MoPair row
+_OFF_T0 = L.MoPair.t0.offset // 4
+_OFF_TILE0 = L.MoPair.tile0.offset // 4
+_OFF_NTILES = L.MoPair.ntiles.offset // 4
 
 _adam_tables = {}
 
@@ -87,6 +91,9 @@ class Pair:
         self.grad_dbg = torch.zeros(self.nv * 3, dtype=torch.float32, device=dev) if debug_grad else None
         self.adam_tab = adam_table(max(self.steps, 1), self.lr, self.b1, self.b2, dev)
         self.loss_history = []
+        self._row = None
+        self._row_steps = None
+        self._tiles = None
 
     def nbytes(self):
         return (self.pos.numel() + self.rest.numel() + self.m.numel() + self.v.numel() + self.sell.numel()) * 4 + \
@@ -99,6 +106,27 @@ class Pair:
     def positions(self):
         """Current positions as float32 [nv,3] (a view-free copy)."""
         return self.pos[self.t & 1, :, :3].contiguous()
+
+    @property
+    def ntiles(self):
+        return tiles_for(self.nslices)
+
+    def row(self):
+        """This pair's MoPair bytes (t0, tile0 and ntiles are set per group)."""
+        if self._row is None or self._row_steps != self.steps:
+            self._row = np.frombuffer(bytes(self.struct(0, 0, 0)), np.uint8).copy()
+            self._row_steps = self.steps
+        return self._row
+
+    def tile_rows(self):
+        """int32 [ntiles, 4] = (pair, first slice, slices, 0) with pair = 0."""
+        if self._tiles is None:
+            nt = self.ntiles
+            t = np.zeros((nt, 4), np.int32)
+            t[:, 1] = np.arange(nt) * SLICES_PER_TILE
+            t[:, 2] = np.minimum(SLICES_PER_TILE, self.nslices - t[:, 1])
+            self._tiles = t
+        return self._tiles
 
     def struct(self, t0, tile0, ntiles):
         p = L.MoPair()
@@ -149,6 +177,7 @@ class StepGroupRunner:
         self._staging = [torch.zeros(nbytes, dtype=torch.uint8).pin_memory() for _ in range(2)]
         self._staging_ev = [None, None]
         self._slot = 0
+        self._tiles_key = None
         self.graph = None
         self.npairs = 0
         self.ntiles = 0
@@ -161,47 +190,53 @@ class StepGroupRunner:
                  ptr(self.tile_loss), 0, s)
 
     def upload(self, pairs, t0s):
-        """Write the pair and tile tables for the next group (async H2D)."""
-        if len(pairs) > self.max_pairs:
-            raise RuntimeError("too many pairs for this runner (%d > %d)" % (len(pairs), self.max_pairs))
-        structs, tiles = [], []
-        for pi, (pr, t0) in enumerate(zip(pairs, t0s)):
-            nt = tiles_for(pr.nslices)
-            structs.append(pr.struct(t0, len(tiles), nt))
-            for k in range(nt):
-                s0 = k * SLICES_PER_TILE
-                tiles.append((pi, s0, min(SLICES_PER_TILE, pr.nslices - s0)))
-        if len(tiles) > self.max_tiles:
-            raise RuntimeError("too many tiles for this runner (%d > %d)" % (len(tiles), self.max_tiles))
+        """Write the pair and tile tables for the next group (async H2D).
+        Each pair's table row and tile rows are built once and cached; the
+        tile table is only re-sent when the list of active pairs changed."""
+        n = len(pairs)
+        if n > self.max_pairs:
+            raise RuntimeError("too many pairs for this runner (%d > %d)" % (n, self.max_pairs))
+        nts = np.fromiter((p.ntiles for p in pairs), np.int64, count=n)
+        total = int(nts.sum()) if n else 0
+        if total > self.max_tiles:
+            raise RuntimeError("too many tiles for this runner (%d > %d)" % (total, self.max_tiles))
+        key = tuple(id(p) for p in pairs)
+        send_tiles = key != self._tiles_key
         slot = self._slot
         self._slot ^= 1
         ev = self._staging_ev[slot]
         if ev is not None:
             ev.synchronize()
         buf = self._staging[slot]
-        base = buf.data_ptr()
-        pb = len(structs) * PAIR_BYTES
-        arr = (L.MoPair * len(structs))(*structs) if structs else None
-        if arr is not None:
-            ctypes.memmove(base, ctypes.addressof(arr), pb)
-        tb = len(tiles) * TILE_BYTES
-        if tiles:
-            t_np = np.zeros((len(tiles), 4), np.int32)
-            t_np[:, :3] = np.asarray(tiles, np.int32)
-            ctypes.memmove(base + self.max_pairs * PAIR_BYTES, t_np.ctypes.data, tb)
-        nt_off = self.max_pairs * PAIR_BYTES + self.max_tiles * TILE_BYTES
-        ctypes.memmove(base + nt_off, np.asarray([len(tiles)], np.int32).ctypes.data, 4)
-        if pb:
+        view = buf.numpy()
+        pb = n * PAIR_BYTES
+        if n:
+            tab = view[:pb].reshape(n, PAIR_BYTES)
+            for i, p in enumerate(pairs):
+                tab[i] = p.row()
+            ints = tab.view(np.int32)
+            tile0 = np.concatenate([[0], np.cumsum(nts)[:-1]])
+            ints[:, _OFF_T0] = np.asarray(t0s, np.int32)
+            ints[:, _OFF_TILE0] = tile0
+            ints[:, _OFF_NTILES] = nts
             self.pairs_dev[:pb].copy_(buf[:pb], non_blocking=True)
-        if tb:
-            self.tiles_dev[:tb].copy_(buf[self.max_pairs * PAIR_BYTES:self.max_pairs * PAIR_BYTES + tb],
-                                      non_blocking=True)
-        self.ntiles_dev.view(torch.uint8).copy_(buf[nt_off:nt_off + 4], non_blocking=True)
+        tb = total * TILE_BYTES
+        t_off = self.max_pairs * PAIR_BYTES
+        nt_off = t_off + self.max_tiles * TILE_BYTES
+        if send_tiles:
+            if total:
+                tiles = view[t_off:t_off + tb].view(np.int32).reshape(total, 4)
+                tiles[:] = np.concatenate([p.tile_rows() for p in pairs])
+                tiles[:, 0] = np.repeat(np.arange(n, dtype=np.int32), nts)
+                self.tiles_dev[:tb].copy_(buf[t_off:t_off + tb], non_blocking=True)
+            view[nt_off:nt_off + 4].view(np.int32)[0] = total
+            self.ntiles_dev.view(torch.uint8).copy_(buf[nt_off:nt_off + 4], non_blocking=True)
+            self._tiles_key = key
         ev = torch.cuda.Event()
         ev.record()
         self._staging_ev[slot] = ev
-        self.npairs = len(structs)
-        self.ntiles = len(tiles)
+        self.npairs = n
+        self.ntiles = total
 
     def run_group(self):
         """Launch S fused steps (graph replay when enabled)."""

@@ -1,0 +1,80 @@
+"""Small, fixed workloads for profiling single kernels with ncu.
+
+    python -m meshode_gb300.profiling step --pairs 64 --groups 1
+        the first `pairs` requests of the serving stream prepared and stepped
+        together: `groups` x 25 launches of k_fused_step with every pair
+        active (plus one warm-up group);
+    python -m meshode_gb300.profiling df --request 1 --repeat 2
+        the distance-field build of one request of the stream, `repeat` times.
+
+Each prints one line with the CUDA-event timing of the measured launches.
+"""
+import argparse
+import sys
+
+import torch
+
+from . import _lib as L
+from . import build as B
+from . import meshgen, serving
+from . import pyDeform as PD
+
+
+def _stream(n, seed=5):
+    specs = meshgen.serving_requests(n=512, seed=seed)[:n]
+    return specs, [meshgen.request_meshes(s) for s in specs]
+
+
+def step(args):
+    specs, meshes = _stream(args.pairs)
+    dev = torch.device("cuda")
+    reqs = serving.requests_from_meshes(meshes, specs, device=dev)
+    for r in reqs:
+        r.steps = 100000
+    eng = serving.ServingEngine(group_steps=25, results_to_host=False)
+    jobs = eng.prepare(reqs)
+    t, nbytes, nv = eng.steady_state(jobs, groups=args.groups)
+    print("k_fused_step: %d pairs, %d vertices, %.4f ms/launch, %.1f GB/s algorithmic (104V+44H)"
+          % (len(jobs), nv, t * 1e3, nbytes / t / 1e9))
+
+
+def df(args):
+    specs, meshes = _stream(args.request + 1)
+    s = specs[args.request]
+    Vs, Fs, Vt, Ft = meshes[args.request]
+    dev = torch.device("cuda")
+    Vd = torch.from_numpy(Vt).to(dev)
+    Fd = torch.from_numpy(Ft).to(dev)
+    method = {"auto": L.MO_DF_AUTO, "brute": L.MO_DF_BRUTE, "lbvh": L.MO_DF_LBVH}[args.method]
+    times = []
+    for _ in range(args.repeat):
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        PD.InitializeDeformTemplate(Vd, Fd, 0, s["N"], df_method=method)
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    print("df build: request %d, N=%d, %d triangles, ms per build %s"
+          % (args.request, s["N"], Ft.shape[0], ", ".join("%.2f" % t for t in times)))
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(prog="python -m meshode_gb300.profiling")
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    a = sub.add_parser("step")
+    a.add_argument("--pairs", type=int, default=64)
+    a.add_argument("--groups", type=int, default=1)
+    b = sub.add_parser("df")
+    b.add_argument("--request", type=int, default=1)
+    b.add_argument("--repeat", type=int, default=2)
+    b.add_argument("--method", default="auto", choices=["auto", "brute", "lbvh"])
+    args = ap.parse_args(argv)
+    B.build()
+    L.require_cuda()
+    {"step": step, "df": df}[args.cmd](args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -334,6 +334,44 @@ class ServingEngine:
         self._timing = []
         return wall
 
+    def prepare(self, requests):
+        """Admit and build every request without stepping (for steady-state
+        measurements of the fused step); returns the jobs."""
+        for r in requests:
+            fused.adam_table(max(r.steps, 1), r.lr, 0.9, 0.999, self.device)
+        jobs = []
+        for r in requests:
+            j = _Job(r, 0)
+            self._phase_a(j)
+            jobs.append(j)
+        torch.cuda.synchronize(self.device)
+        for j in jobs:
+            if not self._phase_b(j):
+                raise RuntimeError("request %s failed: %s" % (j.req.id, j.req.error))
+        torch.cuda.synchronize(self.device)
+        return jobs
+
+    def steady_state(self, jobs, groups=2):
+        """Time `groups` step groups with every prepared pair active: returns
+        (seconds per step, algorithmic bytes per step, vertices)."""
+        pairs = [j.pair for j in jobs]
+        if sum(fused.tiles_for(p.nslices) for p in pairs) > self.runner.max_tiles:
+            raise RuntimeError("too many tiles for one group")
+        self.runner.upload(pairs, [0] * len(pairs))
+        self.runner.run_group()  # warm-up (and graph capture)
+        torch.cuda.synchronize(self.device)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(self.step_stream)
+        for g in range(groups):
+            self.runner.upload(pairs, [self.runner.S * (g + 1)] * len(pairs))
+            self.runner.run_group()
+        e1.record(self.step_stream)
+        torch.cuda.synchronize(self.device)
+        t = e0.elapsed_time(e1) * 1e-3 / (groups * self.runner.S)
+        nbytes = sum(104 * p.nv + 44 * j.nh for p, j in zip(pairs, jobs))
+        return t, nbytes, sum(p.nv for p in pairs)
+
     def step_roofline(self):
         """(algorithmic GB/s of the fused steps, their total seconds)."""
         if self.group_time_s <= 0:
