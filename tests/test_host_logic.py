@@ -1,0 +1,78 @@
+"""Host-side logic that needs no GPU: OBJ reading quirks, argument
+validation of the pyDeform mirror, generators, admission accounting,
+the Chamfer metric."""
+import numpy as np
+import pytest
+import torch
+
+from meshode_gb300 import fused, meshgen, metrics, objio, serving
+from meshode_gb300 import pyDeform as PD
+
+
+def test_obj_reader_quirks(tmp_path):
+    p = tmp_path / "m.obj"
+    lines = ["# comment", "v 0 0 0", "v 1.5 0 0", "vn 0 0 1", "v 0 2 0", "v 0 0 3",
+             "f 1/1/1 2/2/2 3/3/3", "f  1//1 3//3 4//4 2//2", "", "vt 0 0", "f 4 3 2"]
+    p.write_text("\n".join(lines) + "\n" + "v " + "1 " * 200 + "\n" + "v 9 9 9\n")
+    V, F = objio.read_obj(str(p))
+    assert V.shape == (4, 3) and V[1, 0] == 1.5
+    assert F.tolist() == [[0, 1, 2], [0, 2, 3], [3, 2, 1]]   # quads keep 3 corners; long line stops reading
+
+
+def test_obj_roundtrip(tmp_path):
+    V, F = meshgen.icosphere(1)
+    p = tmp_path / "o.obj"
+    PD.SaveMesh(str(p), torch.from_numpy(V.astype(np.float32)), torch.from_numpy(F.astype(np.int32)))
+    V2, F2 = PD.LoadMesh(str(p))
+    assert V2.dtype == torch.float32 and F2.dtype == torch.int32
+    assert np.abs(V2.numpy() - V).max() < 1e-5 and np.array_equal(F2.numpy(), F)
+
+
+def test_validation_errors_without_gpu():
+    with pytest.raises(RuntimeError):
+        PD.DistanceFieldLoss_forward(torch.zeros(5, 3, dtype=torch.float64), 0)
+    with pytest.raises(RuntimeError):
+        PD.DistanceFieldLoss_backward(torch.zeros(5, 4), 0)
+    with pytest.raises(RuntimeError):
+        PD.RigidEdgeLoss_forward(torch.zeros(5, 3), torch.zeros(2, 3, dtype=torch.int64), 0)
+    with pytest.raises(RuntimeError):
+        PD.InitializeDeformTemplate(torch.zeros(5, 3), torch.zeros(0, 3, dtype=torch.int32), 0, 64)
+    with pytest.raises(RuntimeError):
+        PD.InitializeDeformTemplate(torch.zeros(5, 3), torch.zeros(2, 3, dtype=torch.int32), 0, 1)
+    with pytest.raises(NotImplementedError):
+        PD.LoadCadMesh("x.obj")
+
+
+def test_generators():
+    V, F = meshgen.icosphere(3)
+    assert V.shape == (642, 3) and F.shape == (1280, 3)
+    V, F = meshgen.cubesphere(9)
+    assert V.shape == (6 * 81 + 2, 3) and F.shape == (12 * 81, 3)
+    e = np.concatenate([F[:, [0, 1]], F[:, [1, 2]], F[:, [2, 0]]])
+    assert len({tuple(x) for x in e}) == len(e)                      # consistently oriented
+    assert all((b, a) in {tuple(x) for x in e} for a, b in e[:50])    # closed
+    specs = meshgen.serving_requests(n=512)
+    nv = np.array([s["nv"] for s in specs])
+    nt = np.array([s["nt"] for s in specs])
+    assert nv.min() >= 2000 and nv.max() <= 100000 and nt.min() >= 5000 and nt.max() <= 500000
+    assert set(s["N"] for s in specs) == {64, 128}
+    gaps = np.diff([s["arrival"] for s in specs])
+    assert abs(gaps.mean() - 1 / 200.0) < 1e-3
+    a = meshgen.serving_requests(n=8, seed=5)
+    b = meshgen.serving_requests(n=8, seed=5)
+    assert a == b
+
+
+def test_admission_estimate_and_tiles():
+    e1 = serving.estimate_bytes(1000, 2000, 1000, 2000, 64)
+    e2 = serving.estimate_bytes(2000, 4000, 1000, 2000, 64)
+    e3 = serving.estimate_bytes(1000, 2000, 1000, 2000, 128)
+    assert e1 < e2 and e1 < e3
+    assert fused.tiles_for(1) == 1 and fused.tiles_for(8) == 1 and fused.tiles_for(9) == 2
+
+
+def test_chamfer_metric():
+    V, F = meshgen.icosphere(2)
+    assert metrics.chamfer(V, F, V, F, samples=2000) == pytest.approx(0.0, abs=1e-12)
+    d = metrics.chamfer(V, F, V + np.array([0.01, 0, 0]), F, samples=2000)
+    assert 0.005 < d <= 0.0101
