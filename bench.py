@@ -221,6 +221,85 @@ def run_plain_gpu(specs, meshes, ids):
     return time.perf_counter() - t0, outs
 
 
+def df_build_times(specs, meshes, ids):
+    """Warm, isolated DF builds (bbox, normalisation, LBVH/brute build, cell
+    relayout) of the listed requests: CUDA-event ms each."""
+    from meshode_gb300 import pyDeform as PD
+    dev = torch.device("cuda")
+    out = []
+    for i in ids:
+        Vs, Fs, Vt, Ft = meshes[i]
+        Vd, Fd = torch.from_numpy(Vt).to(dev), torch.from_numpy(Ft).to(dev)
+        PD.ReleaseTemplate(PD.InitializeDeformTemplate(Vd, Fd, 0, specs[i]["N"]))
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        pid = PD.InitializeDeformTemplate(Vd, Fd, 0, specs[i]["N"])
+        e1.record()
+        torch.cuda.synchronize()
+        PD.ReleaseTemplate(pid)
+        out.append((specs[i]["N"], Ft.shape[0], e0.elapsed_time(e1)))
+    return out
+
+
+def large_config(threads):
+    """The large-scale configuration: displaced ico-8 target (1,310,720
+    triangles) at 256^3, a 200k-vertex source: DF build ms (GPU; CPU oracle
+    extrapolated from a 0.2% voxel sample) and the fused step's steady state."""
+    from meshode_gb300 import fused, meshgen
+    from meshode_gb300 import pyDeform as PD
+    from oracle import pydeform_oracle as orc  # checker / CPU baseline only
+    dev = torch.device("cuda")
+    Vs, Fs, Vt, Ft = meshgen.large_pair(seed=3)
+    N = 256
+    Vd, Fd = torch.from_numpy(Vt).to(dev), torch.from_numpy(Ft).to(dev)
+    PD.ReleaseTemplate(PD.InitializeDeformTemplate(Vd, Fd, 0, N))
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    pid = PD.InitializeDeformTemplate(Vd, Fd, 0, N)
+    e1.record()
+    torch.cuda.synchronize()
+    gpu_ms = e0.elapsed_time(e1)
+    # DF parity on a voxel sample against the FP64 oracle
+    grid = PD.GetDistanceField(pid).reshape(-1)
+    sc, tr = orc.normalize_params(Vt)
+    Tn = orc.normalized_double(Vt, sc, tr)
+    rng = np.random.Generator(np.random.PCG64(3))
+    vox = rng.choice(N ** 3, size=N ** 3 // 500, replace=False).astype(np.int64)
+    t0 = time.perf_counter()
+    ref = orc.df_build(Tn, Ft, N, voxels=vox, method="bvh", threads=threads)
+    cpu_s = time.perf_counter() - t0
+    err = float(np.abs(grid[torch.from_numpy(vox).to(dev)].double().cpu().numpy() - ref).max())
+    diag = float(np.linalg.norm(Tn.max(0) - Tn.min(0)))
+    # fused step on the 200k-vertex source
+    V = torch.from_numpy(Vs.copy()).to(dev)
+    PD.NormalizeByTemplate(V, pid)
+    PD.StoreRigidityInformation(V, torch.from_numpy(Fs).to(dev), pid)
+    pr = fused.pair_from_template(pid, V, steps=100000)
+    runner = fused.StepGroupRunner(dev, 1, pr.ntiles, group_steps=25)
+    runner.upload([pr], [0])
+    runner.run_group()
+    torch.cuda.synchronize()
+    e0.record()
+    for g in range(4):
+        runner.upload([pr], [25 * (g + 1)])
+        runner.run_group()
+    e1.record()
+    torch.cuda.synchronize()
+    step_ms = e0.elapsed_time(e1) / 100
+    nh = 3 * Fs.shape[0]
+    nbytes = 104 * pr.nv + 44 * nh
+    PD.ReleaseTemplate(pid)
+    return {"target_tris": int(Ft.shape[0]), "N": N, "source_vertices": int(Vs.shape[0]), "half_edges": nh,
+            "df_build_ms": gpu_ms,
+            "df_max_abs_err_over_diag_vs_fp64": err / diag, "df_check_voxels": int(vox.shape[0]),
+            "cpu_df_build_ms_extrapolated": cpu_s * 1e3 * (N ** 3 / vox.shape[0]), "cpu_threads": threads,
+            "step_ms": step_ms, "step_algorithmic_gbs": nbytes / (step_ms * 1e-3) / 1e9}
+
+
 # ---------------------------------------------------------------------------
 def reference_arm(args, world, rank):
     """CPU implementation of the path (oracle port), all host threads."""
@@ -356,6 +435,17 @@ def ours_arm(args, world, rank):
         cpu_baseline = {"value": cpu_rate, "unit": UNIT, "cores": threads, "kind": "port",
                         "sample": "request %s (DF build + %d steps), oracle restatement + torch CPU Adam"
                                   % (cids, args.req_steps)}
+        # DF build ms: a 48-request sample of the stream, and the large configuration
+        dfs = df_build_times(specs, meshes, list(range(min(48, len(specs)))))
+        by_n = {}
+        for n_, t_, ms in dfs:
+            by_n.setdefault(str(n_), []).append(ms)
+        extras["df_build_ms"] = {
+            "stream_sample_mean": float(np.mean([d[2] for d in dfs])),
+            "by_grid": {k: {"mean": float(np.mean(v)), "p50": float(np.median(v)), "max": float(max(v)),
+                            "n": len(v)} for k, v in by_n.items()},
+            "note": "warm, one build at a time: bbox + normalisation + LBVH or brute force + cell relayout"}
+        extras["large_config"] = large_config(threads)
     else:
         cpu_baseline = None
     peak, peak_kind = measured_peaks()

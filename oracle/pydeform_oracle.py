@@ -379,3 +379,17 @@ def rigid_fit(src_V, src_F, pid, steps, lr=1e-3, loss_every=0, threads=None):
             V.grad = rigid_grad(V.data, src_F, pid)
         opt.step()
     return V.detach(), losses
+
+
+def graph_fit(src_V, src_E, pid, steps, rigidity2, lr=1e-3):
+    """The CAD loop (src/python/cad_deform.py:30-37) with GraphLossFunction
+    (graph_loss_layer.py:9-43) and torch.optim.Adam on the CPU."""
+    V = torch.nn.Parameter(src_V.clone())
+    opt = torch.optim.Adam([V], lr=lr)
+    for _ in range(steps):
+        opt.zero_grad()
+        with torch.no_grad():
+            _, g = graph_loss_grad(V.data, src_E, pid, rigidity2)
+            V.grad = g
+        opt.step()
+    return V.detach()

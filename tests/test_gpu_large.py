@@ -1,0 +1,62 @@
+"""The large-scale configuration: displaced ico-8 target (1,310,720
+triangles), 256^3 grid, 200k-vertex source.
+
+* DF against the FP64 oracle on a random 0.1% of the voxels (1e-5 of the
+  bounding-box diagonal);
+* the fused step's total gradient bit for bit against the oracle's
+  RigidLossFunction gradient over all 200k vertices;
+* a few steps against oracle gradients + torch.optim.Adam on the CPU.
+"""
+import numpy as np
+import pytest
+import torch
+
+from meshode_gb300 import fused, meshgen
+from meshode_gb300 import pyDeform as PD
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def large(cuda, orc):
+    Vs, Fs, Vt, Ft = meshgen.large_pair(seed=3)
+    N = 256
+    pid = PD.InitializeDeformTemplate(torch.from_numpy(Vt), torch.from_numpy(Ft), 0, N)
+    V = torch.from_numpy(Vs.copy()).to(cuda)
+    PD.NormalizeByTemplate(V, pid)
+    PD.StoreRigidityInformation(V, torch.from_numpy(Fs).to(cuda), pid)
+    grid = PD.GetDistanceField(pid).reshape(-1).cpu().numpy()
+    opid = orc.InitializeDeformTemplate(Vt, Ft, 0, N, grid=grid)
+    Vc = V.cpu()
+    orc.StoreRigidityInformation(Vc, torch.from_numpy(Fs), opid)
+    yield dict(Vs=Vs, Fs=Fs, Vt=Vt, Ft=Ft, N=N, pid=pid, V=V, Vc=Vc, grid=grid, opid=opid)
+    PD.ReleaseTemplate(pid)
+
+
+def test_large_df_vs_fp64_sample(orc, large):
+    N = large["N"]
+    sc, tr = orc.normalize_params(large["Vt"])
+    Tn = orc.normalized_double(large["Vt"], sc, tr)
+    rng = np.random.Generator(np.random.PCG64(3))
+    vox = rng.choice(N ** 3, size=N ** 3 // 1000, replace=False).astype(np.int64)
+    ref = orc.df_build(Tn, large["Ft"], N, voxels=vox, method="bvh")
+    diag = float(np.linalg.norm(Tn.max(0) - Tn.min(0)))
+    err = np.abs(large["grid"][vox].astype(np.float64) - ref).max()
+    assert err <= 1e-5 * diag, (err, diag)
+
+
+def test_large_fused_gradient_bitexact(orc, large):
+    pr = fused.pair_from_template(large["pid"], large["V"], steps=1, debug_grad=True)
+    runner = fused.StepGroupRunner(large["V"].device, 1, pr.ntiles, group_steps=1, use_graph=False)
+    runner.upload([pr], [0])
+    runner.run_group()
+    g = pr.grad_dbg.view(-1, 3).cpu()
+    ref = orc.rigid_grad(large["Vc"], torch.from_numpy(large["Fs"]), large["opid"])
+    assert torch.equal(g, ref), int((g != ref).sum())
+
+
+def test_large_steps_vs_cpu_adam(orc, large):
+    K = 10
+    out, _ = fused.fused_fit(large["pid"], large["V"], K, group_steps=5)
+    ref, _ = orc.rigid_fit(large["Vc"], torch.from_numpy(large["Fs"]), large["opid"], K)
+    assert (out.cpu() - ref).abs().max().item() <= 1e-6

@@ -76,3 +76,26 @@ def test_chamfer_metric():
     assert metrics.chamfer(V, F, V, F, samples=2000) == pytest.approx(0.0, abs=1e-12)
     d = metrics.chamfer(V, F, V + np.array([0.01, 0, 0]), F, samples=2000)
     assert 0.005 < d <= 0.0101
+
+
+def test_mesh_utilities_restated():
+    from meshode_gb300 import meshops
+    V = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [1e-8, 0, 0], [0, 0, 1]], np.float64)
+    F = np.array([[0, 1, 2], [3, 1, 2], [0, 0, 4], [2, 1, 0], [0, 1, 4]])
+    V2, F2 = meshops.merge_duplex(V, F)
+    # vertex 3 truncates onto vertex 0; face [3,1,2] duplicates [0,1,2], [2,1,0] too; [0,0,4] is degenerate
+    assert V2.shape[0] == 4 and F2.tolist() == [[0, 1, 2], [0, 1, 3]]
+    Vd, Fd = meshops.remove_degenerated(V, np.array([[0, 1, 2], [0, 1, 3], [4, 4, 2]]))
+    assert Fd.tolist() == [[0, 1, 2]]
+    Vr, Fr = meshops.reflection_symmetrize(V[:3], F[:1])
+    assert Vr.shape == (6, 3) and Vr[4, 0] == -1.0 and Fr.tolist() == [[0, 1, 2], [3, 4, 5]]
+    Vs, Fs = meshops.subdivide_to(V[:3], F[:1], 10)
+    assert Vs.shape[0] >= 10 and Fs.shape[0] == 16
+
+
+def test_cli_usage_without_gpu(capsys):
+    from meshode_gb300 import cli
+    assert cli.main(["rigid_deform", "a.obj", "b.obj", "c.obj"]) == 0
+    assert "GRID_RESOLUTION" in capsys.readouterr().out
+    assert cli.main(["cad_deform"]) == 0
+    assert "flow_output" in capsys.readouterr().out
