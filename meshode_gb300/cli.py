@@ -154,7 +154,7 @@ def main(argv=None):
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--flow-every", type=int, default=50)
     ap.add_argument("args", nargs="*")
-    a = ap.parse_args(argv)
+    a = ap.parse_intermixed_args(argv)
     if a.program == "rigid_deform":
         return rigid_deform(a.args, steps=a.steps, lr=a.lr)
     return cad_deform(a.args, steps=a.steps, lr=a.lr, flow_every=a.flow_every)
