@@ -239,6 +239,32 @@ int mo_fused_step(const MoPair* pairs, const MoTile* tiles, const int32_t* ntile
  * positions before step t0+k+1. */
 int mo_pair_loss(const MoPair* pairs, int npairs, int max_tiles, int nlaunch, const float* tile_loss,
                  double* pair_loss, void* stream);
+/* ------------------------------------------------------------------------
+ * Velocity-field ODE deformation (the NeuralODE variant,
+ * src/python/layers/neuralode_fast.py:7-64; here 3 -> m -> m -> m -> 3 with
+ * softplus and fixed-step RK4).  The m x m layers are plain GEMMs done by
+ * the caller (cuBLAS); these are the kernels around them.
+ * ------------------------------------------------------------------------ */
+/* z = x W1^T + b1, h = softplus(z): x [n,3], W1 [m,3], z and h [n,m]
+ * (z may be NULL when only h is needed). */
+int mo_mlp_in(const float* x, int64_t n, const float* W1, const float* b1, int m, float* z, float* h,
+              void* stream);
+/* In place z += b (per column), h = softplus(z): z, h [n,m], b [m]. */
+int mo_bias_softplus(float* z, int64_t n, int m, const float* b, float* h, void* stream);
+/* k = h W4^T + b4 (h [n,m], W4 [3,m]); u = x + a*k; acc = (init_acc ? x : acc)
+ * + w*k -- one RK4 stage's output and update; k, u or acc may be NULL. */
+int mo_mlp_out_rk4(const float* h, int64_t n, int m, const float* W4, const float* b4, const float* x,
+                   float a, float w, int init_acc, float* k, float* u, float* acc, void* stream);
+/* g_z = (g_out W4) * sigmoid(z): the output layer's backward through the last
+ * softplus (g_out [n,3], W4 [3,m], z and g_z [n,m]). */
+int mo_mlp_out_bwd(const float* g_out, int64_t n, int m, const float* W4, const float* z, float* g_z,
+                   void* stream);
+/* In place g *= sigmoid(z) (softplus' = sigmoid). */
+int mo_softplus_bwd(float* g, const float* z, int64_t count, void* stream);
+/* g_x = g_z W1 (accumulate != 0: g_x += g_z W1); g_z [n,m], W1 [m,3]. */
+int mo_mlp_in_bwd(const float* g_z, int64_t n, int m, const float* W1, float* g_x, int accumulate,
+                  void* stream);
+
 /* sizeof(MoPair) and sizeof(MoTile) as compiled (host pointers), so that
  * bindings in other languages can check their struct layout. */
 int mo_abi_sizes(size_t* pair_bytes, size_t* tile_bytes);

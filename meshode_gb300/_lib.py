@@ -71,6 +71,12 @@ _SIGS = {
     "mo_fused_step": (_I, [_P, _P, _P, _I, _I, _P, _I, _P]),
     "mo_pair_loss": (_I, [_P, _I, _I, _I, _P, _P, _P]),
     "mo_abi_sizes": (_I, [ctypes.POINTER(_SZ), ctypes.POINTER(_SZ)]),
+    "mo_mlp_in": (_I, [_P, _I64, _P, _P, _I, _P, _P, _P]),
+    "mo_bias_softplus": (_I, [_P, _I64, _I, _P, _P, _P]),
+    "mo_mlp_out_rk4": (_I, [_P, _I64, _I, _P, _P, _P, _F, _F, _I, _P, _P, _P, _P]),
+    "mo_mlp_out_bwd": (_I, [_P, _I64, _I, _P, _P, _P, _P]),
+    "mo_softplus_bwd": (_I, [_P, _P, _I64, _P]),
+    "mo_mlp_in_bwd": (_I, [_P, _I64, _I, _P, _P, _I, _P]),
     "mo_pack_pos": (_I, [_P, _I64, _P, _P]),
     "mo_unpack_pos": (_I, [_P, _I64, _P, _P]),
 }
