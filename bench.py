@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--plain-sample", type=int, default=6)
     ap.add_argument("--cpu-sample-s", type=float, default=20.0)
     ap.add_argument("--no-extras", action="store_true", help="skip latency/plain/cpu legs")
+    ap.add_argument("--no-autotune", action="store_true", help="fixed kernel choices instead of tuned ones")
     return ap.parse_args()
 
 
@@ -300,6 +301,66 @@ def large_config(threads):
             "step_ms": step_ms, "step_algorithmic_gbs": nbytes / (step_ms * 1e-3) / 1e9}
 
 
+def ode_config():
+    """The velocity-field ODE configuration: 50k-vertex source, MLP
+    3->256->256->256->3 (softplus, Xavier seed 4), 20 RK4 steps, 128^3 grid,
+    rigidity 0.1: ms per optimiser iteration (forward flow + fit loss +
+    checkpointed adjoint + Adam) against torch autograd through the same
+    fp32 model (all activations stored)."""
+    from meshode_gb300 import meshgen, neuralode
+    rng = np.random.Generator(np.random.PCG64(4))
+    Vs, Fs = meshgen.cubesphere_for_vertices(50_000)
+    Vt, Ft = meshgen.icosphere(6)
+    Vt = meshgen.displace(Vt, rng)
+    src_V = torch.from_numpy((Vs * 0.8).astype(np.float32))
+    dfm = neuralode.NeuralODEDeformer(src_V, torch.from_numpy(Fs.astype(np.int32)),
+                                      torch.from_numpy(Vt.astype(np.float32)), torch.from_numpy(Ft.astype(np.int32)),
+                                      grid_resolution=128, rigidity=0.1, hidden=256, steps=20, seed=4)
+    for _ in range(2):
+        dfm.step()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(3):
+        dfm.step()
+    e1.record()
+    torch.cuda.synchronize()
+    ours = e0.elapsed_time(e1) / 3
+    # torch autograd through the same model (stores every activation)
+    W = [p.detach().clone().requires_grad_(True) for p in dfm.params]
+    sp = torch.nn.functional.softplus
+
+    def f(x):
+        return sp(sp(sp(x @ W[0].t() + W[1]) @ W[2].t() + W[3]) @ W[4].t() + W[5]) @ W[6].t() + W[7]
+
+    def torch_iter():
+        x = dfm.x0
+        hh = 1.0 / 20
+        for _ in range(20):
+            k1 = f(x)
+            k2 = f(x + hh / 2 * k1)
+            k3 = f(x + hh / 2 * k2)
+            k4 = f(x + hh * k3)
+            x = x + hh / 6 * (k1 + 2 * k2 + 2 * k3 + k4)
+        neuralode.FitLossFunction.apply(x, dfm.F, dfm.pid, dfm.rigidity2).backward()
+
+    torch_iter()
+    torch.cuda.synchronize()
+    peak0 = torch.cuda.max_memory_allocated()
+    e0.record()
+    for _ in range(3):
+        torch_iter()
+    e1.record()
+    torch.cuda.synchronize()
+    plain = e0.elapsed_time(e1) / 3
+    n = dfm.x0.shape[0]
+    flops = 3 * 80 * 2 * n * (3 * 256 + 2 * 256 * 256 + 256 * 3)  # fwd, recompute, vjp ~ 2x fwd
+    return {"source_vertices": n, "hidden": 256, "rk4_steps": 20, "N": 128,
+            "ms_per_iteration": ours, "torch_autograd_ms_per_iteration": plain,
+            "approx_tflops": flops * 4 / 3 / (ours * 1e-3) / 1e12}
+
+
 # ---------------------------------------------------------------------------
 def reference_arm(args, world, rank):
     """CPU implementation of the path (oracle port), all host threads."""
@@ -348,7 +409,13 @@ def ours_arm(args, world, rank):
         return [serving.Request(r.id, r.srcV, r.srcF, r.tarV, r.tarF, N=r.N, steps=r.steps, arrival=r.arrival)
                 for r in reqs]
 
-    engine = serving.ServingEngine(device=dev, group_steps=args.group_steps, results_to_host=False)
+    # per-bucket kernel choices, tuned once before anything is timed
+    from meshode_gb300 import autotune
+    tuner = None if args.no_autotune else autotune.Autotuner()
+    if tuner is not None:
+        tuner.tune_for(req_dev)
+    engine = serving.ServingEngine(device=dev, group_steps=args.group_steps, results_to_host=False,
+                                   autotuner=tuner)
     for _ in range(args.warmup):
         engine.run(fresh(req_dev))
     engine.group_time_s = engine.group_bytes = 0.0
@@ -376,7 +443,8 @@ def ours_arm(args, world, rank):
     value = world * args.requests * args.steps / t_max
     achieved, step_s = engine.step_roofline()
     # ---- timed: end to end through host buffers ----
-    engine_h = serving.ServingEngine(device=dev, group_steps=args.group_steps, results_to_host=True)
+    engine_h = serving.ServingEngine(device=dev, group_steps=args.group_steps, results_to_host=True,
+                                     autotuner=tuner)
     engine_h.run(fresh(req_host))  # warm-up of this engine (graph capture)
     barrier(world)
     torch.cuda.synchronize()
@@ -446,6 +514,7 @@ def ours_arm(args, world, rank):
                             "n": len(v)} for k, v in by_n.items()},
             "note": "warm, one build at a time: bbox + normalisation + LBVH or brute force + cell relayout"}
         extras["large_config"] = large_config(threads)
+        extras["ode_config"] = ode_config()
     else:
         cpu_baseline = None
     peak, peak_kind = measured_peaks()
@@ -454,7 +523,8 @@ def ours_arm(args, world, rank):
     ss_reqs = fresh(req_dev)
     for r in ss_reqs:
         r.steps = 100000
-    ss_engine = serving.ServingEngine(device=dev, group_steps=args.group_steps, results_to_host=False)
+    ss_engine = serving.ServingEngine(device=dev, group_steps=args.group_steps, results_to_host=False,
+                                      autotuner=tuner)
     ss_jobs = ss_engine.prepare(ss_reqs)
     t_ss, bytes_ss, nv_ss = ss_engine.steady_state(ss_jobs, groups=2)
     del ss_jobs, ss_engine
@@ -478,6 +548,13 @@ def ours_arm(args, world, rank):
                                             "with the concurrent DF builds"}},
         "cpu_baseline": cpu_baseline,
         "gpu_launches": int(launches),
+        "autotune": None if tuner is None else {
+            "df": {k: "%s/%s" % ({1: "brute", 2: "lbvh"}.get(v["method"], v["method"]),
+                                 [n for n, c in autotune.PACKETS.items() if c == v["packet"]][0])
+                   for k, v in sorted(tuner.table["df"].items())},
+            "step": {k: "%s/%d" % ([n for n, c in autotune.LAYOUTS.items() if c == v["layout"]][0],
+                                   v["slices_per_tile"]) for k, v in sorted(tuner.table["step"].items())},
+            "keys": "df: N/log2(triangles); step: N/log2(vertices)"},
         "clocks": clk,
     }
     line.update(extras)

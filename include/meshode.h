@@ -34,6 +34,7 @@ extern "C" {
 
 #define MO_LAYOUT_LINEAR 0 /* [z][y][x] float, 4*N^3 bytes */
 #define MO_LAYOUT_CELL 1   /* per cell (x,y,z < N-1) its 8 corners, 32 B = one sector */
+#define MO_LAYOUT_BRICK4 2 /* 4x4x4 bricks of 256 B, bricks and voxels [z][y][x], N padded to 4 */
 
 #define MO_DF_AUTO 0
 #define MO_DF_BRUTE 1 /* shared-memory-tiled brute force (small targets) */
@@ -107,6 +108,21 @@ int mo_df_build_noalloc(const float* V, int64_t nv, const int32_t* F, int64_t nf
                         const double* params4, float* grid_linear_out, void* stream);
 /* MO_DF_NOALLOC_SCRATCH_BYTES as compiled into the library. */
 size_t mo_df_noalloc_scratch_capacity(void);
+/* Traversal packet shapes: the 32 voxels one warp walks the tree with. */
+#define MO_PACKET_4x4x2 0
+#define MO_PACKET_8x4x1 1
+#define MO_PACKET_4x2x4 2
+#define MO_PACKET_2x4x4 3
+#define MO_PACKET_8x2x2 4
+typedef struct MoDfOptions {
+    int32_t method; /* MO_DF_AUTO, MO_DF_BRUTE or MO_DF_LBVH */
+    int32_t packet; /* MO_PACKET_* for MO_DF_LBVH */
+} MoDfOptions;
+/* mo_df_build with explicit build options (opt == NULL: defaults); the
+ * result does not depend on them, only the speed does. */
+int mo_df_build_ex(const float* V, int64_t nv, const int32_t* F, int64_t nf, int N,
+                   const double* params4, const MoDfOptions* opt, void* scratch, size_t scratch_bytes,
+                   float* grid_linear_out, int32_t* status_out, void* stream);
 /* Method MO_DF_AUTO resolves to (host-side heuristic, exported for tests). */
 int mo_df_method_for(int64_t nf, int N);
 

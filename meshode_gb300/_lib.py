@@ -12,7 +12,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libmeshode.so")
 
 MO_OK, MO_ERR_INVALID, MO_ERR_CUDA, MO_ERR_SCRATCH, MO_ERR_DEVICE = 0, 1, 2, 3, 4
-MO_LAYOUT_LINEAR, MO_LAYOUT_CELL = 0, 1
+MO_LAYOUT_LINEAR, MO_LAYOUT_CELL, MO_LAYOUT_BRICK4 = 0, 1, 2
+MO_PACKET_4x4x2, MO_PACKET_8x4x1, MO_PACKET_4x2x4, MO_PACKET_2x4x4, MO_PACKET_8x2x2 = 0, 1, 2, 3, 4
 MO_DF_AUTO, MO_DF_BRUTE, MO_DF_LBVH = 0, 1, 2
 MO_EDGES_FACES, MO_EDGES_LIST = 0, 1
 MO_TILE_WARPS = 8
@@ -35,6 +36,10 @@ class MoPair(ctypes.Structure):
     ]
 
 
+class MoDfOptions(ctypes.Structure):
+    _fields_ = [("method", ctypes.c_int32), ("packet", ctypes.c_int32)]
+
+
 class MoTile(ctypes.Structure):
     _fields_ = [("pair", ctypes.c_int32), ("slice0", ctypes.c_int32), ("nslices", ctypes.c_int32),
                 ("pad", ctypes.c_int32)]
@@ -51,6 +56,7 @@ _SIGS = {
     "mo_df_build_scratch_bytes": (_SZ, [_I64, _I64, _I, _I]),
     "mo_df_build": (_I, [_P, _I64, _P, _I64, _I, _P, _I, _P, _SZ, _P, _P, _P]),
     "mo_df_method_for": (_I, [_I64, _I]),
+    "mo_df_build_ex": (_I, [_P, _I64, _P, _I64, _I, _P, _P, _P, _SZ, _P, _P, _P]),
     "mo_df_build_noalloc": (_I, [_P, _I64, _P, _I64, _I, _P, _P, _P]),
     "mo_df_noalloc_scratch_capacity": (_SZ, []),
     "mo_lbvh_build": (_I, [_P, _I64, _P, _I64, _P, _P, _SZ, _P, _P, _P, _P, _P, _P]),

@@ -22,7 +22,20 @@ struct DFJet {
 template <int LAYOUT>
 __device__ __forceinline__ void df_corners(const float* __restrict__ grid, int N, int px, int py, int pz,
                                            float c[8]) {
-    if (LAYOUT == MO_LAYOUT_CELL) {
+    if (LAYOUT == MO_LAYOUT_BRICK4) {
+        // 32-bit element offsets: grids up to 2^31 floats (N <= 1280)
+        const int nb = (N + 3) >> 2;
+        int ox[2], oy[2], oz[2];
+#pragma unroll
+        for (int d = 0; d < 2; ++d) {
+            const int x = px + d, y = py + d, z = pz + d;
+            ox[d] = (x >> 2) * 64 + (x & 3);
+            oy[d] = (y >> 2) * nb * 64 + (y & 3) * 4;
+            oz[d] = (z >> 2) * nb * nb * 64 + (z & 3) * 16;
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) c[k] = __ldg(grid + (oz[k >> 2] + oy[(k >> 1) & 1] + ox[k & 1]));
+    } else if (LAYOUT == MO_LAYOUT_CELL) {
         const int64_t cell = ((int64_t)pz * (N - 1) + py) * (int64_t)(N - 1) + px;
         const float4* g4 = reinterpret_cast<const float4*>(grid) + 2 * cell;
         const float4 lo = __ldg(g4), hi = __ldg(g4 + 1);

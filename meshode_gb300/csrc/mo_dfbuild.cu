@@ -364,16 +364,20 @@ __device__ __forceinline__ float box_d2(float px, float py, float pz, float4 lo,
     return dx * dx + dy * dy + dz * dz;
 }
 
+// Packet shapes (voxels per warp along x, y, z; product 32), selectable per
+// launch: MO_PACKET_4x4x2 (default), 8x4x1, 4x2x4, 2x4x4, 8x2x2.
+template <int PX, int PY, int PZ>
 __global__ void __launch_bounds__(TRAV_WARPS * 32) k_df_lbvh(const float4* __restrict__ nodes,
                                                              const float4* __restrict__ tris, int ntri, int N,
                                                              float* __restrict__ grid, int* __restrict__ status) {
     __shared__ int stack[TRAV_WARPS][TRAV_STACK];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int bx = (N + 3) / 4, by = (N + 3) / 4, bz = (N + 1) / 2;
+    static_assert(PX * PY * PZ == 32, "a packet is one warp");
+    const int bx = (N + PX - 1) / PX, by = (N + PY - 1) / PY, bz = (N + PZ - 1) / PZ;
     const int64_t brick = (int64_t)blockIdx.x * TRAV_WARPS + w;
     if (brick >= (int64_t)bx * by * bz) return;  // warp-uniform
     const int ix = (int)(brick % bx), iy = (int)((brick / bx) % by), iz = (int)(brick / ((int64_t)bx * by));
-    const int x = ix * 4 + (lane & 3), y = iy * 4 + ((lane >> 2) & 3), z = iz * 2 + (lane >> 4);
+    const int x = ix * PX + (lane % PX), y = iy * PY + ((lane / PX) % PY), z = iz * PZ + lane / (PX * PY);
     const bool valid = x < N && y < N && z < N;
     const float Nf = (float)N;
     const float px = __fdiv_rn((float)x, Nf), py = __fdiv_rn((float)y, Nf), pz = __fdiv_rn((float)z, Nf);
@@ -433,6 +437,25 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) k_df_lbvh(const float4* __res
         }
     }
     if (valid) grid[((int64_t)z * N + y) * N + x] = __fsqrt_rn(best);
+}
+
+template <int PX, int PY, int PZ>
+static void launch_df_lbvh_shape(const float4* nodes, const float4* tris, int ntri, int N, float* grid, int* status,
+                                 cudaStream_t s) {
+    const int64_t bricks = (int64_t)((N + PX - 1) / PX) * ((N + PY - 1) / PY) * ((N + PZ - 1) / PZ);
+    k_df_lbvh<PX, PY, PZ><<<ceil_div(bricks, TRAV_WARPS), TRAV_WARPS * 32, 0, s>>>(nodes, tris, ntri, N, grid, status);
+    ::mo::note_launch();
+}
+
+static void launch_df_lbvh(int packet, const float4* nodes, const float4* tris, int ntri, int N, float* grid,
+                           int* status, cudaStream_t s) {
+    switch (packet) {
+        case MO_PACKET_8x4x1: launch_df_lbvh_shape<8, 4, 1>(nodes, tris, ntri, N, grid, status, s); break;
+        case MO_PACKET_4x2x4: launch_df_lbvh_shape<4, 2, 4>(nodes, tris, ntri, N, grid, status, s); break;
+        case MO_PACKET_2x4x4: launch_df_lbvh_shape<2, 4, 4>(nodes, tris, ntri, N, grid, status, s); break;
+        case MO_PACKET_8x2x2: launch_df_lbvh_shape<8, 2, 2>(nodes, tris, ntri, N, grid, status, s); break;
+        default: launch_df_lbvh_shape<4, 4, 2>(nodes, tris, ntri, N, grid, status, s); break;
+    }
 }
 
 // Brute force: each thread one voxel, triangles staged through shared memory.
@@ -564,9 +587,12 @@ extern "C" size_t mo_df_build_scratch_bytes(int64_t nv, int64_t nf, int N, int m
     return plan_scratch(nullptr, nv, nf, method).bytes;
 }
 
-extern "C" int mo_df_build(const float* V, int64_t nv, const int32_t* F, int64_t nf, int N, const double* params4,
-                           int method, void* scratch, size_t scratch_bytes, float* grid_out, int32_t* status_out,
-                           void* stream) {
+extern "C" int mo_df_build_ex(const float* V, int64_t nv, const int32_t* F, int64_t nf, int N,
+                              const double* params4, const MoDfOptions* opt, void* scratch, size_t scratch_bytes,
+                              float* grid_out, int32_t* status_out, void* stream) {
+    int method = opt ? opt->method : MO_DF_AUTO;
+    const int packet = opt ? opt->packet : MO_PACKET_4x4x2;
+    MO_CHECK_ARG(packet >= MO_PACKET_4x4x2 && packet <= MO_PACKET_8x2x2, "unknown packet shape %d", packet);
     MO_CHECK_ARG(nv > 0 && nf > 0, "target mesh must have vertices and faces (nv=%lld nf=%lld)", (long long)nv,
                  (long long)nf);
     MO_CHECK_ARG(nf < ((int64_t)1 << 30) && nv < ((int64_t)1 << 31), "target mesh too large");
@@ -611,9 +637,7 @@ extern "C" int mo_df_build(const float* V, int64_t nv, const int32_t* F, int64_t
                 k_karras<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.codes_a, (int)nf, S.nodes, S.parent, S.flags); ::mo::note_launch();
                 k_refit<<<ceil_div(nf, 256), 256, 0, s>>>(S.boxes, (int)nf, S.nodes, S.parent, S.flags, S.rootbox, st); ::mo::note_launch();
             }
-            const int64_t bricks = (int64_t)((N + 3) / 4) * ((N + 3) / 4) * ((N + 1) / 2);
-            k_df_lbvh<<<ceil_div(bricks, TRAV_WARPS), TRAV_WARPS * 32, 0, s>>>(S.nodes, S.tris, (int)nf, N,
-                                                                               grid_out, st); ::mo::note_launch();
+            launch_df_lbvh(packet, S.nodes, S.tris, (int)nf, N, grid_out, st, s);
         }
         e = cudaGetLastError();
         if (e != cudaSuccess) { fail(e, "df build kernels"); break; }
@@ -629,6 +653,15 @@ extern "C" int mo_df_build(const float* V, int64_t nv, const int32_t* F, int64_t
     }
     if (owned) cudaFreeAsync(owned, s);
     return rc;
+}
+
+extern "C" int mo_df_build(const float* V, int64_t nv, const int32_t* F, int64_t nf, int N, const double* params4,
+                           int method, void* scratch, size_t scratch_bytes, float* grid_out, int32_t* status_out,
+                           void* stream) {
+    MoDfOptions opt;
+    opt.method = method;
+    opt.packet = MO_PACKET_4x4x2;
+    return mo_df_build_ex(V, nv, F, nf, N, params4, &opt, scratch, scratch_bytes, grid_out, status_out, stream);
 }
 
 extern "C" int mo_lbvh_build(const float* V, int64_t nv, const int32_t* F, int64_t nf, const double* params4,

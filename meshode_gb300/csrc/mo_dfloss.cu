@@ -34,10 +34,12 @@ static int launch_dfloss(const float* V, int64_t n, const float* grid, int N, in
                          float* grad, int use_mask, float mask_thresh, cudaStream_t s) {
     MO_CHECK_ARG(n >= 0, "negative vertex count");
     MO_CHECK_ARG(N >= 2, "grid resolution must be >= 2 (got %d)", N);
-    MO_CHECK_ARG(layout == MO_LAYOUT_LINEAR || layout == MO_LAYOUT_CELL, "unknown grid layout %d", layout);
+    MO_CHECK_ARG(layout == MO_LAYOUT_LINEAR || layout == MO_LAYOUT_CELL || layout == MO_LAYOUT_BRICK4,
+                 "unknown grid layout %d", layout);
     MO_CHECK_ARG(n == 0 || (V && grid), "null vertex or grid pointer");
     MO_CHECK_ARG(!BWD || n == 0 || grad, "null gradient pointer");
     MO_CHECK_ARG(layout != MO_LAYOUT_CELL || aligned(grid, 16), "cell-layout grid must be 16-byte aligned");
+    MO_CHECK_ARG(layout != MO_LAYOUT_BRICK4 || N <= 1280, "brick layout supports N <= 1280");
     if (n == 0) return MO_OK;
     const int threads = 256;
     const int blocks = ceil_div(n, threads);
@@ -45,6 +47,9 @@ static int launch_dfloss(const float* V, int64_t n, const float* grid, int N, in
     if (layout == MO_LAYOUT_CELL) {
         k_dfloss<MO_LAYOUT_CELL, FWD, BWD><<<blocks, threads, 0, s>>>(V, n, grid, N, Nf, Cf, loss, grad,
                                                                       use_mask, mask_thresh);
+    } else if (layout == MO_LAYOUT_BRICK4) {
+        k_dfloss<MO_LAYOUT_BRICK4, FWD, BWD><<<blocks, threads, 0, s>>>(V, n, grid, N, Nf, Cf, loss, grad,
+                                                                        use_mask, mask_thresh);
     } else {
         k_dfloss<MO_LAYOUT_LINEAR, FWD, BWD><<<blocks, threads, 0, s>>>(V, n, grid, N, Nf, Cf, loss, grad,
                                                                         use_mask, mask_thresh);
@@ -52,6 +57,17 @@ static int launch_dfloss(const float* V, int64_t n, const float* grid, int N, in
     ::mo::note_launch();
     MO_LAUNCH_CHECK("k_dfloss");
     return MO_OK;
+}
+
+// Linear [z][y][x] -> 4x4x4 bricks (padding voxels hold 0; they are never read).
+__global__ void __launch_bounds__(256) k_relayout_brick4(const float* __restrict__ g, int N, float* __restrict__ out) {
+    const int nb = (N + 3) >> 2, P = nb * 4;
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= (int64_t)P * P * P) return;
+    const int x = (int)(v % P), y = (int)((v / P) % P), z = (int)(v / ((int64_t)P * P));
+    const int64_t b = ((int64_t)(z >> 2) * nb + (y >> 2)) * nb + (x >> 2);
+    const float val = (x < N && y < N && z < N) ? g[((int64_t)z * N + y) * N + x] : 0.f;
+    out[b * 64 + (((z & 3) * 4 + (y & 3)) * 4 + (x & 3))] = val;
 }
 
 // Linear [z][y][x] -> per-cell 8 corners (k = (bz<<2)|(by<<1)|bx).
@@ -92,6 +108,10 @@ extern "C" size_t mo_grid_bytes(int N, int layout) {
     if (N < 2) return 0;
     if (layout == MO_LAYOUT_LINEAR) return (size_t)N * N * N * sizeof(float);
     if (layout == MO_LAYOUT_CELL) return (size_t)(N - 1) * (N - 1) * (N - 1) * 8 * sizeof(float);
+    if (layout == MO_LAYOUT_BRICK4) {
+        const size_t nb = (size_t)(N + 3) / 4;
+        return nb * nb * nb * 64 * sizeof(float);
+    }
     return 0;
 }
 
@@ -101,6 +121,12 @@ extern "C" int mo_grid_relayout(const float* grid_linear, int N, int layout, flo
     cudaStream_t s = as_stream(stream);
     if (layout == MO_LAYOUT_LINEAR) {
         MO_CUDA(cudaMemcpyAsync(out, grid_linear, mo_grid_bytes(N, layout), cudaMemcpyDeviceToDevice, s));
+        return MO_OK;
+    }
+    if (layout == MO_LAYOUT_BRICK4) {
+        const int64_t P = (int64_t)((N + 3) / 4) * 4;
+        k_relayout_brick4<<<ceil_div(P * P * P, 256), 256, 0, s>>>(grid_linear, N, out); ::mo::note_launch();
+        MO_LAUNCH_CHECK("k_relayout_brick4");
         return MO_OK;
     }
     MO_CHECK_ARG(layout == MO_LAYOUT_CELL, "unknown grid layout %d", layout);

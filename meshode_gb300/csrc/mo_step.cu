@@ -45,7 +45,7 @@ __device__ __forceinline__ DFJet df_eval_layout(const float* grid, int N, float 
 
 // Every warp owns one 32-vertex slice of a tile and never waits for the
 // other warps of its block.
-__global__ void __launch_bounds__(STEP_THREADS) k_fused_step(const MoPair* __restrict__ pairs,
+__global__ void __launch_bounds__(STEP_THREADS, 4) k_fused_step(const MoPair* __restrict__ pairs,
                                                              const MoTile* __restrict__ tiles,
                                                              const int* __restrict__ ntiles_p, int max_tiles,
                                                              int k, float* __restrict__ tile_loss) {
@@ -79,8 +79,11 @@ __global__ void __launch_bounds__(STEP_THREADS) k_fused_step(const MoPair* __res
         }
         const int N = P.N;
         const float Nf = (float)N, Cf = (float)((double)(N - 1) - 1e-3);
-        const DFJet j = (P.layout == MO_LAYOUT_CELL) ? df_eval_layout<MO_LAYOUT_CELL>(P.grid, N, Nf, Cf, p.x, p.y, p.z)
-                                                     : df_eval_layout<MO_LAYOUT_LINEAR>(P.grid, N, Nf, Cf, p.x, p.y, p.z);
+        const DFJet j = (P.layout == MO_LAYOUT_CELL)
+                            ? df_eval_layout<MO_LAYOUT_CELL>(P.grid, N, Nf, Cf, p.x, p.y, p.z)
+                            : (P.layout == MO_LAYOUT_BRICK4)
+                                  ? df_eval_layout<MO_LAYOUT_BRICK4>(P.grid, N, Nf, Cf, p.x, p.y, p.z)
+                                  : df_eval_layout<MO_LAYOUT_LINEAR>(P.grid, N, Nf, Cf, p.x, p.y, p.z);
         const float dsq = MUL(j.d, j.d);
         float gdx = df_grad_component(j.d, j.gx);
         float gdy = df_grad_component(j.d, j.gy);

@@ -52,7 +52,7 @@ class Pair:
 
     def __init__(self, grid, N, layout, V, csr, nh, rest, steps, lr=1e-3, betas=(0.9, 0.999), eps=1e-8,
                  w_edge=1.0, mask_thresh=None, grad_scale=1.0, debug_grad=False, stream=None, slice_ptr=None,
-                 nrec=None):
+                 nrec=None, slices_per_tile=SLICES_PER_TILE):
         """V: normalised source vertices, float32 [nv,3] on the device (the
         optimiser's start).  csr/nh: the edge CSR buffer and half-edge count.
         rest: float32 [nv,3] positions the rest offsets were taken from (the V
@@ -64,6 +64,11 @@ class Pair:
         self.grid = grid
         self.N = int(N)
         self.layout = int(layout)
+        if self.layout == L.MO_LAYOUT_BRICK4 and self.N > 1280:
+            raise RuntimeError("the brick layout supports grids up to 1280^3")
+        if not 1 <= int(slices_per_tile) <= L.MO_TILE_WARPS:
+            raise RuntimeError("slices per tile must be in [1, %d]" % L.MO_TILE_WARPS)
+        self.slices_per_tile = int(slices_per_tile)
         self.nv = int(V.shape[0])
         self.nslices = (self.nv + 31) // 32
         self.steps = int(steps)
@@ -109,7 +114,7 @@ class Pair:
 
     @property
     def ntiles(self):
-        return tiles_for(self.nslices)
+        return tiles_for(self.nslices, self.slices_per_tile)
 
     def row(self):
         """This pair's MoPair bytes (t0, tile0 and ntiles are set per group)."""
@@ -121,10 +126,10 @@ class Pair:
     def tile_rows(self):
         """int32 [ntiles, 4] = (pair, first slice, slices, 0) with pair = 0."""
         if self._tiles is None:
-            nt = self.ntiles
+            nt, spt = self.ntiles, self.slices_per_tile
             t = np.zeros((nt, 4), np.int32)
-            t[:, 1] = np.arange(nt) * SLICES_PER_TILE
-            t[:, 2] = np.minimum(SLICES_PER_TILE, self.nslices - t[:, 1])
+            t[:, 1] = np.arange(nt) * spt
+            t[:, 2] = np.minimum(spt, self.nslices - t[:, 1])
             self._tiles = t
         return self._tiles
 
@@ -155,8 +160,8 @@ class Pair:
         return p
 
 
-def tiles_for(nslices):
-    return (nslices + SLICES_PER_TILE - 1) // SLICES_PER_TILE
+def tiles_for(nslices, slices_per_tile=SLICES_PER_TILE):
+    return (nslices + slices_per_tile - 1) // slices_per_tile
 
 
 class StepGroupRunner:
@@ -286,7 +291,7 @@ def fused_fit(pid, src_V_norm, steps, lr=1e-3, group_steps=25, use_graph=True, w
     reference's plain Adam loop, rigid_deform.py:34-41).  Returns
     (final normalised positions [nv,3] on the device, per-step losses or None)."""
     pr = pair_from_template(pid, src_V_norm, steps, lr=lr, w_edge=w_edge, mask_thresh=mask_thresh)
-    runner = StepGroupRunner(pr.device, 1, tiles_for(pr.nslices), group_steps=group_steps, use_graph=use_graph)
+    runner = StepGroupRunner(pr.device, 1, pr.ntiles, group_steps=group_steps, use_graph=use_graph)
     losses = []
     while not pr.done:
         runner.upload([pr], [pr.t])

@@ -24,6 +24,7 @@ Each pair's arithmetic depends only on its own state, so a result is the
 same, bit for bit, whether the request ran alone or in any mix.
 """
 import collections
+import ctypes
 import time
 
 import numpy as np
@@ -62,10 +63,11 @@ class Request:
 
 
 def estimate_bytes(nv, nf_src, nv_tar, nf_tar, N, layout=L.MO_LAYOUT_CELL):
-    """Peak device bytes one request holds from admission to retirement."""
+    """Peak device bytes one request holds from admission to retirement
+    (the grid counted in the largest layout)."""
     lib = L.lib()
     nh = 3 * nf_src
-    grid = lib.mo_grid_bytes(N, layout) + 4 * N ** 3
+    grid = max(lib.mo_grid_bytes(N, lay) for lay in (L.MO_LAYOUT_CELL, L.MO_LAYOUT_BRICK4, layout)) + 4 * N ** 3
     scratch = lib.mo_df_build_scratch_bytes(nv_tar, nf_tar, N, L.MO_DF_AUTO)
     meshes = 12 * (nv + nf_src + nv_tar + nf_tar)
     edges = lib.mo_edge_csr_bytes(nv, nf_src, L.MO_EDGES_FACES)
@@ -76,7 +78,7 @@ def estimate_bytes(nv, nf_src, nv_tar, nf_tar, N, layout=L.MO_LAYOUT_CELL):
 
 class _Job:
     __slots__ = ("req", "bytes", "phase", "ev", "host", "nv", "nh", "Vd", "Fd", "params", "grid", "csr", "off",
-                 "slice_ptr", "status", "pair", "out_dev", "out_host", "stream")
+                 "slice_ptr", "status", "pair", "out_dev", "out_host", "stream", "layout", "spt")
 
     def __init__(self, req, nbytes):
         self.req = req
@@ -90,7 +92,7 @@ class _Job:
 class ServingEngine:
     def __init__(self, device=None, hbm_budget_bytes=None, max_pairs=512, max_tiles=None, group_steps=25,
                  layout=L.MO_LAYOUT_CELL, use_graph=True, max_building=8, results_to_host=True, lr=1e-3,
-                 build_streams=2):
+                 build_streams=2, autotuner=None):
         L.require_cuda()
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
         free, total = torch.cuda.mem_get_info(self.device)
@@ -107,6 +109,8 @@ class ServingEngine:
         self._next_build = 0
         self.step_stream = torch.cuda.current_stream(self.device)
         self.max_building = int(max_building)
+        # per-request DF build options and step layout / tile width
+        self.autotuner = autotuner
         self.results_to_host = bool(results_to_host)
         self.in_use = 0
         self.peak_in_use = 0
@@ -142,18 +146,25 @@ class ServingEngine:
             call("mo_bbox", ptr(Td), Td.shape[0], ptr(bbox), s)
             call("mo_norm_params", ptr(bbox), ptr(job.params), s)
             N = req.N
-            nb = lib.mo_df_build_scratch_bytes(Td.shape[0], TFd.shape[0], N, L.MO_DF_AUTO)
+            if self.autotuner is not None:
+                method, packet = self.autotuner.df_options(N, TFd.shape[0])
+                job.layout, job.spt = self.autotuner.step_options(N, nv)
+            else:
+                method, packet = L.MO_DF_AUTO, L.MO_PACKET_4x4x2
+                job.layout, job.spt = self.layout, fused.SLICES_PER_TILE
+            opt = L.MoDfOptions(method, packet)
+            nb = lib.mo_df_build_scratch_bytes(Td.shape[0], TFd.shape[0], N, method)
             scratch = torch.empty(int(nb), dtype=torch.uint8, device=self.device)
             glin = torch.empty(N ** 3, dtype=torch.float32, device=self.device)
-            call("mo_df_build", ptr(Td), Td.shape[0], ptr(TFd), TFd.shape[0], N, ptr(job.params), L.MO_DF_AUTO,
-                 ptr(scratch), nb, ptr(glin), ptr(job.status[0:1]), s)
+            call("mo_df_build_ex", ptr(Td), Td.shape[0], ptr(TFd), TFd.shape[0], N, ptr(job.params),
+                 ctypes.byref(opt), ptr(scratch), nb, ptr(glin), ptr(job.status[0:1]), s)
             del scratch
-            if self.layout == L.MO_LAYOUT_LINEAR:
+            if job.layout == L.MO_LAYOUT_LINEAR:
                 job.grid = glin
             else:
-                job.grid = torch.empty(lib.mo_grid_bytes(N, self.layout) // 4, dtype=torch.float32,
+                job.grid = torch.empty(lib.mo_grid_bytes(N, job.layout) // 4, dtype=torch.float32,
                                        device=self.device)
-                call("mo_grid_relayout", ptr(glin), N, self.layout, ptr(job.grid), s)
+                call("mo_grid_relayout", ptr(glin), N, job.layout, ptr(job.grid), s)
                 del glin
             del Td, TFd
             call("mo_normalize", ptr(Vd), nv, ptr(job.params), 0, s)
@@ -181,9 +192,9 @@ class ServingEngine:
         req = job.req
         with torch.cuda.stream(job.stream):
             # the rest offsets are taken from the normalised source itself
-            job.pair = fused.Pair(job.grid, req.N, self.layout, job.Vd, job.csr, job.nh, job.Vd, req.steps,
+            job.pair = fused.Pair(job.grid, req.N, job.layout, job.Vd, job.csr, job.nh, job.Vd, req.steps,
                                   lr=req.lr, w_edge=req.w_edge, stream=job.stream, slice_ptr=job.slice_ptr,
-                                  nrec=st[2])
+                                  nrec=st[2], slices_per_tile=job.spt)
             job.csr = job.off = job.Fd = job.Vd = None
             for t in (job.grid, job.pair.pos, job.pair.rest, job.pair.m, job.pair.v, job.pair.sell,
                       job.pair.slice_ptr, job.params):
@@ -355,7 +366,7 @@ class ServingEngine:
         """Time `groups` step groups with every prepared pair active: returns
         (seconds per step, algorithmic bytes per step, vertices)."""
         pairs = [j.pair for j in jobs]
-        if sum(fused.tiles_for(p.nslices) for p in pairs) > self.runner.max_tiles:
+        if sum(p.ntiles for p in pairs) > self.runner.max_tiles:
             raise RuntimeError("too many tiles for one group")
         self.runner.upload(pairs, [0] * len(pairs))
         self.runner.run_group()  # warm-up (and graph capture)

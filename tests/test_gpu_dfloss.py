@@ -64,8 +64,8 @@ def _same(a, b):
     return bool(eq.all()), int((~eq).sum())
 
 
-@pytest.mark.parametrize("N", [16, 64])
-@pytest.mark.parametrize("layout", [L.MO_LAYOUT_LINEAR, L.MO_LAYOUT_CELL])
+@pytest.mark.parametrize("N", [16, 63, 64])
+@pytest.mark.parametrize("layout", [L.MO_LAYOUT_LINEAR, L.MO_LAYOUT_CELL, L.MO_LAYOUT_BRICK4])
 def test_dfloss_bitexact(cuda, orc, N, layout):
     pid = _template(N)
     grid = PD.GetDistanceField(pid).cpu().numpy().reshape(-1)

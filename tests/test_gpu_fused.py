@@ -50,7 +50,7 @@ def _pair(cuda, orc, level=3, N=32, seed=1, graph=False):
 def test_fused_gradient_bitexact_rigid(cuda, orc):
     pid, opid, Vs, F = _pair(cuda, orc)
     pr = fused.pair_from_template(pid, Vs, steps=1, debug_grad=True)
-    runner = fused.StepGroupRunner(cuda, 1, fused.tiles_for(pr.nslices), group_steps=1, use_graph=False)
+    runner = fused.StepGroupRunner(cuda, 1, pr.ntiles, group_steps=1, use_graph=False)
     runner.upload([pr], [0])
     runner.run_group()
     g = pr.grad_dbg.view(-1, 3).cpu().numpy()
@@ -63,7 +63,7 @@ def test_fused_gradient_bitexact_graph_mask(cuda, orc):
     rig2 = float(torch.tensor(0.7 * 0.7, dtype=torch.float32))
     thresh = float(np.float32(0.5 * 0.03 * 0.03))
     pr = fused.pair_from_template(pid, Vs, steps=1, debug_grad=True, w_edge=rig2, mask_thresh=thresh)
-    runner = fused.StepGroupRunner(cuda, 1, fused.tiles_for(pr.nslices), group_steps=1, use_graph=False)
+    runner = fused.StepGroupRunner(cuda, 1, pr.ntiles, group_steps=1, use_graph=False)
     runner.upload([pr], [0])
     runner.run_group()
     g = pr.grad_dbg.view(-1, 3).cpu().numpy()
@@ -97,7 +97,7 @@ def test_alone_vs_mix_bitexact(cuda, orc):
     prs = [fused.pair_from_template(pid, Vs, steps=K) for pid, _, Vs, _ in built]
     # staggered: the second pair joins later and the third has fewer steps
     prs[2].steps = K - 7
-    max_tiles = sum(fused.tiles_for(p.nslices) for p in prs)
+    max_tiles = sum(p.ntiles for p in prs)
     runner = fused.StepGroupRunner(cuda, 3, max_tiles, group_steps=5)
     active = [prs[0], prs[2]]
     for g in range(8):

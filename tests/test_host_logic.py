@@ -99,3 +99,9 @@ def test_cli_usage_without_gpu(capsys):
     assert "GRID_RESOLUTION" in capsys.readouterr().out
     assert cli.main(["cad_deform"]) == 0
     assert "flow_output" in capsys.readouterr().out
+
+
+def test_autotune_buckets():
+    from meshode_gb300 import autotune
+    assert autotune.t_bucket(5000) == 12 and autotune.t_bucket(8192) == 13
+    assert autotune.v_bucket(1) == 0 and autotune.v_bucket(100000) == 16
