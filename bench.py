@@ -319,6 +319,8 @@ def ode_config():
     for _ in range(2):
         dfm.step()
     torch.cuda.synchronize()
+    base = torch.cuda.memory_allocated()
+    torch.cuda.reset_peak_memory_stats()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record()
@@ -327,6 +329,7 @@ def ode_config():
     e1.record()
     torch.cuda.synchronize()
     ours = e0.elapsed_time(e1) / 3
+    ours_mem = torch.cuda.max_memory_allocated() - base
     # torch autograd through the same model (stores every activation)
     W = [p.detach().clone().requires_grad_(True) for p in dfm.params]
     sp = torch.nn.functional.softplus
@@ -347,18 +350,25 @@ def ode_config():
 
     torch_iter()
     torch.cuda.synchronize()
-    peak0 = torch.cuda.max_memory_allocated()
+    base = torch.cuda.memory_allocated()
+    torch.cuda.reset_peak_memory_stats()
     e0.record()
     for _ in range(3):
         torch_iter()
     e1.record()
     torch.cuda.synchronize()
     plain = e0.elapsed_time(e1) / 3
+    plain_mem = torch.cuda.max_memory_allocated() - base
     n = dfm.x0.shape[0]
-    flops = 3 * 80 * 2 * n * (3 * 256 + 2 * 256 * 256 + 256 * 3)  # fwd, recompute, vjp ~ 2x fwd
+    eval_flops = 2 * n * (3 * 256 + 2 * 256 * 256 + 256 * 3)
+    # 80 evaluations forward, 80 recomputed and 80 back-propagated (~2x) in the adjoint
+    flops = eval_flops * (80 + 80 + 2 * 80)
     return {"source_vertices": n, "hidden": 256, "rk4_steps": 20, "N": 128,
-            "ms_per_iteration": ours, "torch_autograd_ms_per_iteration": plain,
-            "approx_tflops": flops * 4 / 3 / (ours * 1e-3) / 1e12}
+            "ms_per_iteration": ours, "peak_extra_mem_gb": ours_mem / 1e9,
+            "torch_autograd_ms_per_iteration": plain, "torch_autograd_peak_extra_mem_gb": plain_mem / 1e9,
+            "tflops": flops / (ours * 1e-3) / 1e12,
+            "note": "checkpointed adjoint: recomputes each RK4 step's activations (4/3 of the FLOPs) to hold "
+                    "one step's activations instead of all 80 stage evaluations'"}
 
 
 # ---------------------------------------------------------------------------

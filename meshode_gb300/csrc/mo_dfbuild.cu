@@ -140,13 +140,20 @@ __device__ Tri make_tri(const float* __restrict__ Vn, int i0, int i1, int i2, fl
     return t;
 }
 
+// The query arithmetic is written with explicit fmaf / __fmul_rn / __fadd_rn
+// so that every kernel that inlines it (LBVH traversal, brute force) rounds
+// identically and the two build methods give the same grid bit for bit.
+__device__ __forceinline__ float dot3e(float ax, float ay, float az, float bx, float by, float bz) {
+    return fmaf(az, bz, fmaf(ay, by, __fmul_rn(ax, bx)));
+}
+
 __device__ __forceinline__ float seg3_d2(float px, float py, float pz, float4 a, float4 b, float inv_l2) {
-    const float ex = b.x - a.x, ey = b.y - a.y, ez = b.z - a.z;
-    const float apx = px - a.x, apy = py - a.y, apz = pz - a.z;
-    float t = dot3(apx, apy, apz, ex, ey, ez) * inv_l2;
+    const float ex = __fsub_rn(b.x, a.x), ey = __fsub_rn(b.y, a.y), ez = __fsub_rn(b.z, a.z);
+    const float apx = __fsub_rn(px, a.x), apy = __fsub_rn(py, a.y), apz = __fsub_rn(pz, a.z);
+    float t = __fmul_rn(dot3e(apx, apy, apz, ex, ey, ez), inv_l2);
     t = fminf(fmaxf(t, 0.f), 1.f);
-    const float qx = apx - t * ex, qy = apy - t * ey, qz = apz - t * ez;
-    return dot3(qx, qy, qz, qx, qy, qz);
+    const float qx = fmaf(-t, ex, apx), qy = fmaf(-t, ey, apy), qz = fmaf(-t, ez, apz);
+    return dot3e(qx, qy, qz, qx, qy, qz);
 }
 
 // Squared distance from p to the triangle.  `cut` is this lane's current
@@ -155,31 +162,33 @@ __device__ __forceinline__ float seg3_d2(float px, float py, float pz, float4 a,
 // FLT_MAX returned.  The record is warp-uniform, so both branches are too.
 __device__ __forceinline__ float tri_d2(float px, float py, float pz, const Tri& T, float cut) {
     if (T.r3.w != 0.f) {
-        const float qx = px - T.r0.x, qy = py - T.r0.y, qz = pz - T.r0.z;
-        const float h = dot3(qx, qy, qz, T.r3.x, T.r3.y, T.r3.z);
-        const float h2 = h * h;
+        const float qx = __fsub_rn(px, T.r0.x), qy = __fsub_rn(py, T.r0.y), qz = __fsub_rn(pz, T.r0.z);
+        const float h = dot3e(qx, qy, qz, T.r3.x, T.r3.y, T.r3.z);
+        const float h2 = __fmul_rn(h, h);
         if (!__any_sync(0xffffffffu, h2 < cut)) return FLT_MAX;
-        const float x = dot3(qx, qy, qz, T.r1.x, T.r1.y, T.r1.z);
-        const float y = dot3(qx, qy, qz, T.r2.x, T.r2.y, T.r2.z);
+        const float x = dot3e(qx, qy, qz, T.r1.x, T.r1.y, T.r1.z);
+        const float y = dot3e(qx, qy, qz, T.r2.x, T.r2.y, T.r2.z);
         const float bx = T.r0.w, cx = T.r1.w, cy = T.r2.w, ebx = T.r4.w;
+        const float y2 = __fmul_rn(y, y);
         // A-B along the x axis
-        float t = fminf(fmaxf(x * T.r4.x, 0.f), 1.f);
-        float dx = x - t * bx;
-        float d = dx * dx + y * y;
+        float t = fminf(fmaxf(__fmul_rn(x, T.r4.x), 0.f), 1.f);
+        float dx = fmaf(-t, bx, x);
+        float d = fmaf(dx, dx, y2);
         // A-C
-        t = fminf(fmaxf((x * cx + y * cy) * T.r4.y, 0.f), 1.f);
-        dx = x - t * cx;
-        float dy = y - t * cy;
-        d = fminf(d, dx * dx + dy * dy);
+        t = fminf(fmaxf(__fmul_rn(fmaf(x, cx, __fmul_rn(y, cy)), T.r4.y), 0.f), 1.f);
+        dx = fmaf(-t, cx, x);
+        float dy = fmaf(-t, cy, y);
+        d = fminf(d, fmaf(dx, dx, __fmul_rn(dy, dy)));
         // B-C
-        const float xb = x - bx;
-        t = fminf(fmaxf((xb * ebx + y * cy) * T.r4.z, 0.f), 1.f);
-        dx = xb - t * ebx;
-        dy = y - t * cy;
-        d = fminf(d, dx * dx + dy * dy);
+        const float xb = __fsub_rn(x, bx);
+        t = fminf(fmaxf(__fmul_rn(fmaf(xb, ebx, __fmul_rn(y, cy)), T.r4.z), 0.f), 1.f);
+        dx = fmaf(-t, ebx, xb);
+        dy = fmaf(-t, cy, y);
+        d = fminf(d, fmaf(dx, dx, __fmul_rn(dy, dy)));
         // inside: left of A->B, B->C and C->A (counter-clockwise in the frame)
-        const bool inside = (y >= 0.f) && (ebx * y - cy * xb >= 0.f) && (cy * x - cx * y >= 0.f);
-        return h2 + (inside ? 0.f : d);
+        const bool inside = (y >= 0.f) && (fmaf(ebx, y, -__fmul_rn(cy, xb)) >= 0.f) &&
+                            (fmaf(cy, x, -__fmul_rn(cx, y)) >= 0.f);
+        return inside ? h2 : __fadd_rn(h2, d);
     }
     float d = seg3_d2(px, py, pz, T.r0, T.r1, T.r4.x);
     d = fminf(d, seg3_d2(px, py, pz, T.r1, T.r2, T.r4.y));
@@ -355,6 +364,10 @@ __global__ void k_refit(const float4* __restrict__ boxes, int n, float4* nodes, 
 // a child is visited when any lane's box distance beats that lane's best.
 // ---------------------------------------------------------------------------
 constexpr int TRAV_WARPS = 4;
+constexpr float kSlack = 2e-6f;
+
+// (sqrt(best) + kSlack)^2: the squared-distance bound a box must beat.
+__device__ __forceinline__ float slack_bound(float best) { return best + kSlack * (2.f * sqrtf(best) + kSlack); }
 constexpr int TRAV_STACK = 64;
 
 __device__ __forceinline__ float box_d2(float px, float py, float pz, float4 lo, float4 hi) {
@@ -382,6 +395,12 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) k_df_lbvh(const float4* __res
     const float Nf = (float)N;
     const float px = __fdiv_rn((float)x, Nf), py = __fdiv_rn((float)y, Nf), pz = __fdiv_rn((float)z, Nf);
     float best = valid ? FLT_MAX : -1.0f;
+    // Boxes are visited while their fp32 distance is within kSlack (in
+    // distance units) of the lane's best: the rounding of the box bound can
+    // exceed a triangle's computed distance by far less than that, so no
+    // triangle that could lower `best` is skipped and the result is the exact
+    // minimum of the computed distances, whatever the visit order.
+    float lim = valid ? FLT_MAX : -1.0f;
     const unsigned FULL = 0xffffffffu;
     if (ntri == 1) {
         const float t = tri_d2(px, py, pz, load_tri(tris, 0), best);
@@ -401,16 +420,16 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) k_df_lbvh(const float4* __res
             const float4 a = __ldg(nd), b = __ldg(nd + 1), c = __ldg(nd + 2), d = __ldg(nd + 3);
             const int L = __float_as_int(a.w), R = __float_as_int(b.w);
             const float dl = box_d2(px, py, pz, a, b), dr = box_d2(px, py, pz, c, d);
-            bool wl = __any_sync(FULL, dl < best);
-            bool wr = __any_sync(FULL, dr < best);
+            bool wl = __any_sync(FULL, dl < lim);
+            bool wr = __any_sync(FULL, dr < lim);
             if (wl && L < 0) {
                 const float t = tri_d2(px, py, pz, load_tri(tris, ~L), best);
-                if (valid) best = fminf(best, t);
+                if (valid && t < best) { best = t; lim = slack_bound(best); }
                 wl = false;
             }
             if (wr && R < 0) {
                 const float t = tri_d2(px, py, pz, load_tri(tris, ~R), best);
-                if (valid) best = fminf(best, t);
+                if (valid && t < best) { best = t; lim = slack_bound(best); }
                 wr = false;
             }
             if (wl && wr) {
