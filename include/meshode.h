@@ -255,6 +255,108 @@ int mo_fused_step(const MoPair* pairs, const MoTile* tiles, const int32_t* ntile
  * positions before step t0+k+1. */
 int mo_pair_loss(const MoPair* pairs, int npairs, int max_tiles, int nlaunch, const float* tile_loss,
                  double* pair_loss, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Serving pool: admit / step / retire deformation requests.  A request is one
+ * run of the reference's rigid_deform loop (src/python/rigid_deform.py:25-44:
+ * InitializeDeformTemplate, NormalizeByTemplate, StoreRigidityInformation,
+ * `steps` Adam steps of RigidLossFunction, Finalize) on its own source and
+ * target.  The pool admits requests FIFO against an HBM byte budget, builds
+ * each on one of its build streams (copies, DF build, CSR, sliced-ELL records;
+ * memory from a stream-ordered pool), steps every active pair with one
+ * replay of a captured CUDA graph of group_steps mo_fused_step launches per
+ * mo_pool_progress call, and retires a pair (denormalised result in device
+ * memory, final loss) right after the group in which its last step ran.  A
+ * result is bit-identical whether its request ran alone or in any mix.
+ * A pool is driven by one host thread; it has its own non-blocking streams.
+ * No counterpart in the reference (its loop is one pair, synchronous).
+ * ------------------------------------------------------------------------ */
+typedef struct MoPool MoPool;
+
+typedef struct MoPoolConfig {
+    uint64_t hbm_budget_bytes; /* 0: 60% of the device's free memory at creation */
+    int32_t max_pairs;         /* requests building, active or retiring at once */
+    int32_t max_tiles;         /* tiles (<= 8 slices of 32 vertices) stepped at once */
+    int32_t group_steps;       /* optimiser steps per group (one graph replay) */
+    int32_t use_graph;         /* capture the group as a CUDA graph */
+    int32_t max_building;      /* requests in their build phases at once (0: 8) */
+    int32_t build_streams;     /* 0: 2 */
+    int32_t layout;            /* default grid layout (MO_LAYOUT_*) */
+    int32_t slices_per_tile;   /* default tile width, 1..8 (0: 8) */
+} MoPoolConfig;
+
+typedef struct MoRequest {
+    const float* srcV;   /* [nv,3] raw source vertices */
+    const int32_t* srcF; /* [nf,3] source faces (the rigidity edges) */
+    const float* tarV;   /* [ntv,3] raw target vertices */
+    const int32_t* tarF; /* [ntf,3] target faces */
+    int64_t nv, nf, ntv, ntf;
+    int32_t inputs_on_host; /* the four arrays are host memory (else device) */
+    int32_t N;              /* grid resolution */
+    int32_t steps;          /* Adam steps */
+    float w_edge;           /* edge-loss weight (lambda^2 of the rigid CLI) */
+    double lr;              /* Adam learning rate (betas 0.9/0.999, eps 1e-8) */
+    int32_t layout;         /* -1: the pool's default */
+    int32_t slices_per_tile;/* 0: the pool's default */
+    int32_t df_method;      /* MO_DF_AUTO / BRUTE / LBVH */
+    int32_t df_packet;      /* MO_PACKET_* */
+} MoRequest;
+
+#define MO_REQ_FAILED (-1)
+#define MO_REQ_QUEUED 0
+#define MO_REQ_BUILDING 1
+#define MO_REQ_ACTIVE 2
+#define MO_REQ_DONE 3
+
+typedef struct MoPoolStats {
+    int64_t submitted, done, failed;
+    int64_t groups;         /* group replays issued */
+    int64_t fused_launches; /* mo_fused_step launches issued (captured ones counted per replay) */
+    uint64_t bytes_in_use;  /* admission estimate of the requests holding memory */
+    uint64_t peak_bytes;
+    int32_t queued, building, active, retiring;
+    int32_t active_tiles;
+    int32_t pad;
+} MoPoolStats;
+
+int mo_pool_create(const MoPoolConfig* cfg, MoPool** pool_out);
+int mo_pool_destroy(MoPool* pool);
+/* Queue a request.  The input arrays must stay valid and unchanged until the
+ * request is finished (DONE or FAILED).  Checks sizes and options on the host;
+ * invalid meshes (a face index out of range) fail the request later. */
+int mo_pool_submit(MoPool* pool, const MoRequest* req, int64_t* id_out);
+/* Admit, advance builds, run one group over the active pairs, collect
+ * retirements.  block != 0: when nothing is active, wait for the oldest build
+ * or retirement before returning.  n_finished_out: requests DONE or FAILED so far. */
+int mo_pool_progress(MoPool* pool, int block, int64_t* n_finished_out);
+/* Progress until every submitted request is finished (or, on hold, built). */
+int mo_pool_wait(MoPool* pool);
+/* Pop up to max_ids ids of requests finished since the last call, in order. */
+int mo_pool_completed(MoPool* pool, int64_t* ids, int max_ids, int* n_out);
+int mo_pool_state(MoPool* pool, int64_t id, int32_t* state_out);
+/* The failure message of a FAILED request (empty otherwise). */
+int mo_pool_error(MoPool* pool, int64_t id, char* buf, size_t buf_bytes);
+/* Copy a DONE request's fitted vertices [nv,3]: V_out denormalised (as
+ * Finalize returns them), V_normalized_out in the target-normalised frame;
+ * either may be NULL; host or device memory per out_on_host.  loss_out
+ * (host, optional): the layer loss evaluated in the last step.  Synchronous. */
+int mo_pool_result(MoPool* pool, int64_t id, float* V_out, float* V_normalized_out, int out_on_host,
+                   double* loss_out);
+/* Forget a finished request and recycle its result memory. */
+int mo_pool_release(MoPool* pool, int64_t id);
+/* hold != 0: progress admits and builds but does not step (steady-state
+ * measurements: build everything, then mo_pool_run_groups). */
+int mo_pool_set_hold(MoPool* pool, int hold);
+/* Record CUDA events around each group for mo_pool_group_time. */
+int mo_pool_set_timing(MoPool* pool, int enable);
+/* Run `groups` groups over the active pairs now (ignores hold). */
+int mo_pool_run_groups(MoPool* pool, int groups);
+/* Total device time (ms) of the timed groups since the last call and their
+ * algorithmic bytes (104 per vertex + 44 per half-edge per pair-step). */
+int mo_pool_group_time(MoPool* pool, double* ms_out, double* bytes_out);
+int mo_pool_stats(MoPool* pool, MoPoolStats* out);
+/* The pool's step stream (a cudaStream_t). */
+int mo_pool_step_stream(MoPool* pool, void** stream_out);
 /* ------------------------------------------------------------------------
  * Velocity-field ODE deformation (the NeuralODE variant,
  * src/python/layers/neuralode_fast.py:7-64; here 3 -> m -> m -> m -> 3 with

@@ -17,6 +17,7 @@ MO_PACKET_4x4x2, MO_PACKET_8x4x1, MO_PACKET_4x2x4, MO_PACKET_2x4x4, MO_PACKET_8x
 MO_DF_AUTO, MO_DF_BRUTE, MO_DF_LBVH = 0, 1, 2
 MO_EDGES_FACES, MO_EDGES_LIST = 0, 1
 MO_TILE_WARPS = 8
+MO_REQ_FAILED, MO_REQ_QUEUED, MO_REQ_BUILDING, MO_REQ_ACTIVE, MO_REQ_DONE = -1, 0, 1, 2, 3
 
 _P = ctypes.c_void_p
 _I = ctypes.c_int
@@ -43,6 +44,28 @@ class MoDfOptions(ctypes.Structure):
 class MoTile(ctypes.Structure):
     _fields_ = [("pair", ctypes.c_int32), ("slice0", ctypes.c_int32), ("nslices", ctypes.c_int32),
                 ("pad", ctypes.c_int32)]
+
+
+class MoPoolConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_pairs", ctypes.c_int32),
+                ("max_tiles", ctypes.c_int32), ("group_steps", ctypes.c_int32), ("use_graph", ctypes.c_int32),
+                ("max_building", ctypes.c_int32), ("build_streams", ctypes.c_int32), ("layout", ctypes.c_int32),
+                ("slices_per_tile", ctypes.c_int32)]
+
+
+class MoRequest(ctypes.Structure):
+    _fields_ = [("srcV", _P), ("srcF", _P), ("tarV", _P), ("tarF", _P),
+                ("nv", _I64), ("nf", _I64), ("ntv", _I64), ("ntf", _I64),
+                ("inputs_on_host", ctypes.c_int32), ("N", ctypes.c_int32), ("steps", ctypes.c_int32),
+                ("w_edge", _F), ("lr", ctypes.c_double), ("layout", ctypes.c_int32),
+                ("slices_per_tile", ctypes.c_int32), ("df_method", ctypes.c_int32), ("df_packet", ctypes.c_int32)]
+
+
+class MoPoolStats(ctypes.Structure):
+    _fields_ = [("submitted", _I64), ("done", _I64), ("failed", _I64), ("groups", _I64),
+                ("fused_launches", _I64), ("bytes_in_use", ctypes.c_uint64), ("peak_bytes", ctypes.c_uint64),
+                ("queued", ctypes.c_int32), ("building", ctypes.c_int32), ("active", ctypes.c_int32),
+                ("retiring", ctypes.c_int32), ("active_tiles", ctypes.c_int32), ("pad", ctypes.c_int32)]
 
 
 # name -> (restype, argtypes)
@@ -85,6 +108,22 @@ _SIGS = {
     "mo_mlp_in_bwd": (_I, [_P, _I64, _I, _P, _P, _I, _P]),
     "mo_pack_pos": (_I, [_P, _I64, _P, _P]),
     "mo_unpack_pos": (_I, [_P, _I64, _P, _P]),
+    "mo_pool_create": (_I, [_P, _P]),
+    "mo_pool_destroy": (_I, [_P]),
+    "mo_pool_submit": (_I, [_P, _P, _P]),
+    "mo_pool_progress": (_I, [_P, _I, _P]),
+    "mo_pool_wait": (_I, [_P]),
+    "mo_pool_completed": (_I, [_P, _P, _I, _P]),
+    "mo_pool_state": (_I, [_P, _I64, _P]),
+    "mo_pool_error": (_I, [_P, _I64, _P, _SZ]),
+    "mo_pool_result": (_I, [_P, _I64, _P, _P, _I, _P]),
+    "mo_pool_release": (_I, [_P, _I64]),
+    "mo_pool_set_hold": (_I, [_P, _I]),
+    "mo_pool_set_timing": (_I, [_P, _I]),
+    "mo_pool_run_groups": (_I, [_P, _I]),
+    "mo_pool_group_time": (_I, [_P, _P, _P]),
+    "mo_pool_stats": (_I, [_P, _P]),
+    "mo_pool_step_stream": (_I, [_P, _P]),
 }
 
 _lib = None

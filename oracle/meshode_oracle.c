@@ -564,3 +564,30 @@ EXPORT void orc_karras(const uint32_t* k, int n, int* left, int* right) {
         right[i] = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
     }
 }
+
+/* ------------------------------------------------------------------------ */
+/* torch.optim.Adam, one step of one parameter tensor (torch/optim/adam.py   */
+/* _single_tensor_adam, the loop of rigid_deform.py:32,39), restated with   */
+/* one IEEE rounding per tensor operation:                                   */
+/*   exp_avg.lerp_(grad, 1-b1)        m = fma(1-b1, g - m, m)                */
+/*   exp_avg_sq.mul_(b2).addcmul_(grad, grad, value=1-b2)                     */
+/*                                    v = v*b2 + ((1-b2)*g)*g                */
+/*   denom = exp_avg_sq.sqrt() / bc2_sqrt + eps                               */
+/*   param.addcdiv_(exp_avg, denom, value=-step_size)                         */
+/*                                    p = fma(-step_size, m/denom, p)        */
+/* step_size = lr/(1-b1^t) and bc2_sqrt = sqrt(1-b2^t) come from the caller, */
+/* computed in double like adam.py's host arithmetic.  lerp and addcdiv are  */
+/* single fused multiply-adds as in ATen's lerp for weights below 0.5; the   */
+/* torch CPU kernels may round their vectorised and tail lanes differently, */
+/* so this restatement agrees with torch CPU to about an ulp per step.       */
+/* ------------------------------------------------------------------------ */
+EXPORT void orc_adam_step(float* p, const float* g, float* m, float* v, int64_t n, float omb1, float b2,
+                          float omb2, float eps, float step_size, float bc2s) {
+    for (int64_t i = 0; i < n; ++i) {
+        const float gi = g[i];
+        m[i] = fmaf(omb1, gi - m[i], m[i]);
+        v[i] = v[i] * b2 + (omb2 * gi) * gi;
+        const float denom = sqrtf(v[i]) / bc2s + eps;
+        p[i] = fmaf(-step_size, m[i] / denom, p[i]);
+    }
+}

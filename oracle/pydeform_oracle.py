@@ -50,6 +50,8 @@ def lib():
         L.orc_karras.argtypes = [P, ctypes.c_int, P, P]
         L.orc_trunc_i32.restype = ctypes.c_int
         L.orc_trunc_i32.argtypes = [ctypes.c_float]
+        F = ctypes.c_float
+        L.orc_adam_step.argtypes = [P, P, P, P, i64, F, F, F, F, F, F]
         _lib = L
     return _lib
 
@@ -364,32 +366,70 @@ def graph_loss_grad(V, E, pid, rigidity2):
     return loss, gD + gR * r2
 
 
-def rigid_fit(src_V, src_F, pid, steps, lr=1e-3, loss_every=0, threads=None):
-    """Adam loop of rigid_deform.py:32-41 on CPU, returns (V, losses)."""
+class ExactAdam:
+    """torch.optim.Adam([V], lr) (betas 0.9/0.999, eps 1e-8) with the update
+    restated in C, one IEEE rounding per tensor op (orc_adam_step); the bias
+    corrections are computed in Python double exactly as adam.py does."""
+
+    def __init__(self, V, lr=1e-3, betas=(0.9, 0.999), eps=1e-8):
+        self.V = V
+        self.lr, self.b1, self.b2, self.eps = float(lr), float(betas[0]), float(betas[1]), float(eps)
+        self.m = np.zeros(V.numel(), np.float32)
+        self.v = np.zeros(V.numel(), np.float32)
+        self.t = 0
+
+    def step(self, grad):
+        self.t += 1
+        step = float(self.t)
+        step_size = self.lr / (1 - self.b1 ** step)
+        bc2s = (1 - self.b2 ** step) ** 0.5
+        p = self.V.detach().numpy().reshape(-1)
+        g = np.ascontiguousarray(grad.detach().numpy().reshape(-1), np.float32)
+        lib().orc_adam_step(_p(p), _p(g), _p(self.m), _p(self.v), p.size, 1 - self.b1, self.b2, 1 - self.b2,
+                             self.eps, step_size, bc2s)
+
+
+def _optimizer(V, lr, adam):
+    if adam == "torch":
+        return torch.optim.Adam([V], lr=lr)
+    if adam == "exact":
+        return ExactAdam(V, lr=lr)
+    raise ValueError("adam must be 'torch' or 'exact'")
+
+
+def _adam_step(opt, V, g):
+    if isinstance(opt, ExactAdam):
+        opt.step(g)
+    else:
+        opt.zero_grad()
+        V.grad = g
+        opt.step()
+
+
+def rigid_fit(src_V, src_F, pid, steps, lr=1e-3, loss_every=0, threads=None, adam="torch"):
+    """Adam loop of rigid_deform.py:32-41 on CPU, returns (V, losses).
+    adam="torch": torch.optim.Adam on the CPU; "exact": ExactAdam."""
     if threads is not None:
         torch.set_num_threads(threads)
     V = torch.nn.Parameter(src_V.clone())
-    opt = torch.optim.Adam([V], lr=lr)
+    opt = _optimizer(V, lr, adam)
     losses = []
     for it in range(steps):
-        opt.zero_grad()
         with torch.no_grad():
             if loss_every and it % loss_every == 0:
                 losses.append(float(rigid_loss(V.data, src_F, pid)))
-            V.grad = rigid_grad(V.data, src_F, pid)
-        opt.step()
+            g = rigid_grad(V.data, src_F, pid)
+            _adam_step(opt, V, g)
     return V.detach(), losses
 
 
-def graph_fit(src_V, src_E, pid, steps, rigidity2, lr=1e-3):
+def graph_fit(src_V, src_E, pid, steps, rigidity2, lr=1e-3, adam="torch"):
     """The CAD loop (src/python/cad_deform.py:30-37) with GraphLossFunction
-    (graph_loss_layer.py:9-43) and torch.optim.Adam on the CPU."""
+    (graph_loss_layer.py:9-43) and Adam on the CPU (adam as in rigid_fit)."""
     V = torch.nn.Parameter(src_V.clone())
-    opt = torch.optim.Adam([V], lr=lr)
+    opt = _optimizer(V, lr, adam)
     for _ in range(steps):
-        opt.zero_grad()
         with torch.no_grad():
             _, g = graph_loss_grad(V.data, src_E, pid, rigidity2)
-            V.grad = g
-        opt.step()
+            _adam_step(opt, V, g)
     return V.detach()

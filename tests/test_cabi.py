@@ -66,3 +66,52 @@ def test_argument_errors_are_reported_without_gpu():
     assert rc == L.MO_ERR_INVALID
     rc = lib.mo_edge_offsets(None, 10, None, 5, 9, None, None)
     assert rc == L.MO_ERR_INVALID and b"kind" in lib.mo_last_error()
+
+
+STRUCTS = {"MoPair": L.MoPair, "MoTile": L.MoTile, "MoDfOptions": L.MoDfOptions,
+           "MoPoolConfig": L.MoPoolConfig, "MoRequest": L.MoRequest, "MoPoolStats": L.MoPoolStats}
+
+
+def test_struct_offsets_match_c_compiler(tmp_path):
+    """Every field offset and struct size of the ctypes mirror equals what a C
+    compiler makes of include/meshode.h."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        import pytest
+        pytest.skip("no C compiler")
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "meshode.h"', "int main(void) {"]
+    for name, cls in STRUCTS.items():
+        lines.append('printf("%s %%zu\\n", sizeof(%s));' % (name, name))
+        for fname, _ in cls._fields_:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (name, fname, name, fname))
+    lines.append("return 0; }")
+    src = tmp_path / "abi.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "abi"
+    subprocess.run([cc, "-std=c99", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)], check=True)
+    out = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                         check=True).stdout.splitlines())
+    for name, cls in STRUCTS.items():
+        assert int(out[name]) == ctypes.sizeof(cls), name
+        for fname, _ in cls._fields_:
+            assert int(out["%s.%s" % (name, fname)]) == getattr(cls, fname).offset, (name, fname)
+
+
+def test_pool_argument_errors_without_gpu():
+    B.build()
+    lib = L.lib()
+    assert lib.mo_pool_create(None, None) == L.MO_ERR_INVALID
+    cfg = L.MoPoolConfig(max_pairs=0, max_tiles=10, group_steps=5)
+    out = ctypes.c_void_p()
+    assert lib.mo_pool_create(ctypes.byref(cfg), ctypes.byref(out)) == L.MO_ERR_INVALID
+    assert b"sizes" in lib.mo_last_error() and not out.value
+    cfg = L.MoPoolConfig(max_pairs=4, max_tiles=10, group_steps=5, layout=9)
+    assert lib.mo_pool_create(ctypes.byref(cfg), ctypes.byref(out)) == L.MO_ERR_INVALID
+    assert b"layout" in lib.mo_last_error()
+    req = L.MoRequest()
+    nid = ctypes.c_int64()
+    assert lib.mo_pool_submit(None, ctypes.byref(req), ctypes.byref(nid)) == L.MO_ERR_INVALID
+    assert lib.mo_pool_progress(None, 0, None) == L.MO_ERR_INVALID
+    assert lib.mo_pool_destroy(None) == L.MO_OK

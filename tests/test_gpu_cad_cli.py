@@ -3,8 +3,8 @@ against their jittered copies plus a noisy plane, 128^3 grid, rigidity 1,
 source resampled to >= 5000 vertices) and the command-line front ends.
 
 GraphLossFunction semantics (src/python/layers/graph_loss_layer.py:9-43): the
-fused GPU loop against the oracle loop (CPU, same grid) within 1e-6 after 30
-steps and within the Chamfer bar after 300; the plain GPU GraphLossLayer loop
+fused GPU loop against the oracle loop (CPU, same grid, op-by-op Adam) bit
+for bit after 30 steps and within the Chamfer bar after 300; the plain GPU GraphLossLayer loop
 (torch Adam on CUDA) within the Chamfer bar.
 """
 import numpy as np
@@ -40,10 +40,13 @@ def cad(cuda, orc):
 
 
 def test_cad_fused_vs_oracle(orc, cad):
+    """Bit-identical 30-step trajectory against the oracle loop with the
+    op-by-op Adam restatement (torch's CPU Adam differs by about an ulp per
+    step, which the d < 0.03 mask can amplify at a vertex on its edge)."""
     r2 = float(torch.tensor(1.0 * 1.0, dtype=torch.float32))
     out, _ = fused.fused_fit(cad["pid"], cad["V"], 30, group_steps=10, w_edge=r2, mask_thresh=MASK)
-    ref = orc.graph_fit(cad["Vc"], torch.from_numpy(cad["E"]), cad["opid"], 30, r2)
-    assert (out.cpu() - ref).abs().max().item() <= 1e-6
+    ref = orc.graph_fit(cad["Vc"], torch.from_numpy(cad["E"]), cad["opid"], 30, r2, adam="exact")
+    assert torch.equal(out.cpu(), ref), (out.cpu() - ref).abs().max().item()
 
 
 def test_cad_chamfer_300_steps(orc, cad):

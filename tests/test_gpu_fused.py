@@ -3,9 +3,10 @@
 * The total gradient of a fused step equals the oracle's
   RigidLossFunction / GraphLossFunction gradient bit for bit
   (rigid_loss_layer.py:20-27, graph_loss_layer.py:33-43).
-* Positions after several steps match the oracle gradients driven by
-  torch.optim.Adam on the CPU within 1e-6 (the Adam arithmetic itself is not
-  bit-identical: torch's CPU kernels may fuse multiply-adds).
+* Positions after several steps equal the oracle loop with the op-by-op
+  Adam restatement bit for bit, and match the oracle gradients driven by
+  torch.optim.Adam on the CPU within 1e-6 (torch's CPU kernels round some
+  lanes differently).
 * The loss of each step matches the layer loss within rtol 1e-5.
 * A pair stepped alone and inside a mix of other pairs gives bit-identical
   results (the serving invariance).
@@ -71,6 +72,15 @@ def test_fused_gradient_bitexact_graph_mask(cuda, orc):
     assert np.array_equal(g, ref.numpy()), int((g != ref.numpy()).sum())
     L = runner.pair_losses(1)[0, 0].item()
     assert abs(L - float(loss)) <= 1e-5 * abs(float(loss)) + 1e-9
+
+
+def test_fused_trajectory_bitexact_vs_exact_adam(cuda, orc):
+    """40 fused steps equal the oracle loop with the op-by-op Adam
+    restatement bit for bit (gradients and update both exact)."""
+    pid, opid, Vs, F = _pair(cuda, orc)
+    out, _ = fused.fused_fit(pid, Vs, 40, group_steps=8)
+    ref, _ = orc.rigid_fit(Vs, F, opid, 40, adam="exact")
+    assert torch.equal(out.cpu(), ref), (out.cpu() - ref).abs().max().item()
 
 
 @pytest.mark.parametrize("use_graph", [False, True])

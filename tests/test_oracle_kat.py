@@ -172,3 +172,54 @@ def test_adam_table_matches_torch():
         bc2 = 1 - 0.999 ** st
         assert tab[t - 1, 0] == np.float32(1e-3 / bc1)
         assert tab[t - 1, 1] == np.float32(bc2 ** 0.5)
+
+
+def _f32_round(x):
+    """Correctly rounded float32 of an exact rational (ties to even)."""
+    from fractions import Fraction
+    f = np.float32(float(x))
+    best = None
+    for c in (np.nextafter(f, np.float32(-np.inf)), f, np.nextafter(f, np.float32(np.inf))):
+        d = abs(Fraction(float(c)) - x)
+        if best is None or d < best[0] or (d == best[0] and int(np.float32(c).view(np.uint32)) % 2 == 0):
+            best = (d, c)
+    return np.float32(best[1])
+
+
+def test_exact_adam_definition_and_torch(orc):
+    """orc_adam_step is torch's _single_tensor_adam op sequence with one
+    rounding per op (checked against exact rational arithmetic), and stays
+    within a few ulps of torch.optim.Adam on the CPU over many steps."""
+    import torch
+    from fractions import Fraction as Fr
+    rng = np.random.Generator(np.random.PCG64(12))
+    n = 37
+    V0 = rng.standard_normal(n).astype(np.float32)
+    grads = [rng.standard_normal(n).astype(np.float32) * np.float32(10.0 ** rng.integers(-3, 2))
+             for _ in range(60)]
+    Vt = torch.nn.Parameter(torch.from_numpy(V0.copy()))
+    opt = torch.optim.Adam([Vt], lr=1e-3)
+    Ve = torch.nn.Parameter(torch.from_numpy(V0.copy()))
+    ex = orc.ExactAdam(Ve, lr=1e-3)
+    # first step against the definition, element by element
+    p, m, v = V0.copy(), np.zeros(n, np.float32), np.zeros(n, np.float32)
+    g = grads[0]
+    step_size = np.float32(1e-3 / (1 - 0.9 ** 1.0))
+    bc2s = np.float32((1 - 0.999 ** 1.0) ** 0.5)
+    omb1, b2, omb2, eps = np.float32(1 - 0.9), np.float32(0.999), np.float32(1 - 0.999), np.float32(1e-8)
+    for i in range(n):
+        m[i] = _f32_round(Fr(float(omb1)) * Fr(float(np.float32(g[i] - m[i]))) + Fr(float(m[i])))
+        v[i] = np.float32(v[i] * b2) + np.float32(np.float32(omb2 * g[i]) * g[i])
+        denom = np.float32(np.float32(np.sqrt(v[i])) / bc2s) + eps
+        q = np.float32(m[i] / denom)
+        p[i] = _f32_round(Fr(-float(step_size)) * Fr(float(q)) + Fr(float(p[i])))
+    ex.step(torch.from_numpy(g))
+    assert np.array_equal(Ve.detach().numpy(), p)
+    for g in grads[1:]:
+        ex.step(torch.from_numpy(g))
+    for g in grads:
+        opt.zero_grad()
+        Vt.grad = torch.from_numpy(g.copy())
+        opt.step()
+    diff = np.abs(Ve.detach().numpy() - Vt.detach().numpy()).max()
+    assert diff <= 1e-6, diff
