@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--cpu-sample-s", type=float, default=20.0)
     ap.add_argument("--no-extras", action="store_true", help="skip latency/plain/cpu legs")
     ap.add_argument("--no-autotune", action="store_true", help="fixed kernel choices instead of tuned ones")
+    ap.add_argument("--engine", default="native", choices=["native", "python"],
+                    help="serving loop: the C++ pool behind mo_pool_* or the Python engine")
     return ap.parse_args()
 
 
@@ -424,8 +426,26 @@ def ours_arm(args, world, rank):
     tuner = None if args.no_autotune else autotune.Autotuner()
     if tuner is not None:
         tuner.tune_for(req_dev)
-    engine = serving.ServingEngine(device=dev, group_steps=args.group_steps, results_to_host=False,
-                                   autotuner=tuner)
+    from meshode_gb300 import pool
+
+    # one HBM budget for every engine of this run, fixed before any of them
+    # holds memory (a native pool keeps freed blocks until trimmed; torch's
+    # caching allocator keeps them for the Python engine)
+    budget = int(torch.cuda.mem_get_info(dev)[0] * 0.6)
+
+    def make_engine(results_to_host, max_pairs=512):
+        if args.engine == "native":
+            return pool.NativePool(device=dev, group_steps=args.group_steps, results_to_host=results_to_host,
+                                   autotuner=tuner, max_pairs=max_pairs, hbm_budget_bytes=budget)
+        return serving.ServingEngine(device=dev, group_steps=args.group_steps, results_to_host=results_to_host,
+                                     autotuner=tuner, max_pairs=max_pairs, hbm_budget_bytes=budget)
+
+    def fused_launches(eng):
+        if args.engine == "native":
+            return eng.launches  # every mo_fused_step launch, graph replays included
+        return eng.runner.launches if eng.runner.use_graph else 0
+
+    engine = make_engine(False)
     for _ in range(args.warmup):
         engine.run(fresh(req_dev))
     engine.group_time_s = engine.group_bytes = 0.0
@@ -435,7 +455,7 @@ def ours_arm(args, world, rank):
     barrier(world)
     torch.cuda.synchronize()
     n0 = lib.mo_launch_count()
-    g0 = engine.runner.launches
+    g0 = fused_launches(engine)
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record()
@@ -448,13 +468,15 @@ def ours_arm(args, world, rank):
     barrier(world)
     clk = clocks.stop()
     t_dev = ev0.elapsed_time(ev1) * 1e-3
-    launches = (lib.mo_launch_count() - n0) + (engine.runner.launches - g0 if engine.runner.use_graph else 0)
+    # direct launches counted by the library, plus the fused steps replayed from graphs
+    launches = (lib.mo_launch_count() - n0) + (fused_launches(engine) - g0)
     t_max = max_over_ranks(t_dev, world)
     value = world * args.requests * args.steps / t_max
     achieved, step_s = engine.step_roofline()
     # ---- timed: end to end through host buffers ----
-    engine_h = serving.ServingEngine(device=dev, group_steps=args.group_steps, results_to_host=True,
-                                     autotuner=tuner)
+    if args.engine == "native":
+        engine.trim()
+    engine_h = make_engine(True)
     engine_h.run(fresh(req_host))  # warm-up of this engine (graph capture)
     barrier(world)
     torch.cuda.synchronize()
@@ -467,6 +489,8 @@ def ours_arm(args, world, rank):
     torch.cuda.synchronize()
     barrier(world)
     t_e2e = max_over_ranks(e0.elapsed_time(e1) * 1e-3, world)
+    if args.engine == "native":
+        engine_h.close()
     e2e_value = world * args.requests * args.steps / t_e2e
     if rank != 0:
         return
@@ -533,11 +557,16 @@ def ours_arm(args, world, rank):
     ss_reqs = fresh(req_dev)
     for r in ss_reqs:
         r.steps = 100000
-    ss_engine = serving.ServingEngine(device=dev, group_steps=args.group_steps, results_to_host=False,
-                                      autotuner=tuner)
-    ss_jobs = ss_engine.prepare(ss_reqs)
-    t_ss, bytes_ss, nv_ss = ss_engine.steady_state(ss_jobs, groups=2)
-    del ss_jobs, ss_engine
+    ss_engine = make_engine(False, max_pairs=len(ss_reqs) + 1)
+    if args.engine == "native":
+        engine.close()
+        t_ss, bytes_ss, nv_ss = ss_engine.steady_state(ss_reqs, groups=2)
+        ss_engine.close()
+    else:
+        ss_jobs = ss_engine.prepare(ss_reqs)
+        t_ss, bytes_ss, nv_ss = ss_engine.steady_state(ss_jobs, groups=2)
+        del ss_jobs
+    del ss_engine
     achieved_ss = bytes_ss / t_ss / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -545,6 +574,7 @@ def ours_arm(args, world, rank):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "requests": args.requests, "req_steps": args.req_steps,
                    "group_steps": args.group_steps, "parallelism": "replicas" if world > 1 else "single",
+                   "engine": "mo_pool (C ABI)" if args.engine == "native" else "python",
                    "l2": "inputs larger than L2 (~1.3 GB meshes, ~20 GB grids per stream)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "kernel": "k_fused_step", "achieved": achieved_ss, "peak": peak,

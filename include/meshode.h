@@ -115,14 +115,28 @@ size_t mo_df_noalloc_scratch_capacity(void);
 #define MO_PACKET_2x4x4 3
 #define MO_PACKET_8x2x2 4
 typedef struct MoDfOptions {
-    int32_t method; /* MO_DF_AUTO, MO_DF_BRUTE or MO_DF_LBVH */
-    int32_t packet; /* MO_PACKET_* for MO_DF_LBVH */
+    int32_t method;   /* MO_DF_AUTO, MO_DF_BRUTE or MO_DF_LBVH */
+    int32_t packet;   /* MO_PACKET_* for MO_DF_LBVH */
+    float band;       /* 0: exact grid.  > 0: voxels at distance >= band store
+                       * band, except the two lowest layers along each axis
+                       * (x, y or z <= 1), which stay exact; see mo_df_loss_band */
+    int32_t reserved; /* 0 */
 } MoDfOptions;
-/* mo_df_build with explicit build options (opt == NULL: defaults); the
- * result does not depend on them, only the speed does. */
+/* mo_df_build with explicit build options (opt == NULL: defaults).  method
+ * and packet change only the speed, never the grid. */
 int mo_df_build_ex(const float* V, int64_t nv, const int32_t* F, int64_t nf, int N,
                    const double* params4, const MoDfOptions* opt, void* scratch, size_t scratch_bytes,
                    float* grid_linear_out, int32_t* status_out, void* stream);
+/* The smallest band that leaves DistanceFieldLoss unchanged for every input:
+ * 0.2 + sqrt(3)/N + 1e-3.  UniformGrid::DistanceFloat (uniformgrid.cc:
+ * 147-148) returns 0 when the in-range trilinear value exceeds 0.2; grid
+ * values are 1-Lipschitz, so a cell with a corner at or beyond the band has
+ * every corner above 0.2 + 1e-3 - rounding and interpolates above 0.2 from
+ * either grid, and the only lookups that extrapolate (coordinates in
+ * (-1/N, 0)) read the exact lowest layers.  The serving pool builds with this
+ * band: its losses and results are bit-identical to an exact grid's, and the
+ * build skips most of the far field. */
+float mo_df_loss_band(int N);
 /* Method MO_DF_AUTO resolves to (host-side heuristic, exported for tests). */
 int mo_df_method_for(int64_t nf, int N);
 
@@ -300,6 +314,8 @@ typedef struct MoRequest {
     int32_t slices_per_tile;/* 0: the pool's default */
     int32_t df_method;      /* MO_DF_AUTO / BRUTE / LBVH */
     int32_t df_packet;      /* MO_PACKET_* */
+    float df_band;          /* < 0: mo_df_loss_band(N); 0: exact grid; > 0: this band */
+    int32_t reserved;       /* 0 */
 } MoRequest;
 
 #define MO_REQ_FAILED (-1)
@@ -355,6 +371,9 @@ int mo_pool_run_groups(MoPool* pool, int groups);
  * algorithmic bytes (104 per vertex + 44 per half-edge per pair-step). */
 int mo_pool_group_time(MoPool* pool, double* ms_out, double* bytes_out);
 int mo_pool_stats(MoPool* pool, MoPoolStats* out);
+/* Return freed device memory the pool keeps for reuse to the device, down to
+ * keep_bytes (synchronises the pool's streams). */
+int mo_pool_trim(MoPool* pool, uint64_t keep_bytes);
 /* The pool's step stream (a cudaStream_t). */
 int mo_pool_step_stream(MoPool* pool, void** stream_out);
 /* ------------------------------------------------------------------------

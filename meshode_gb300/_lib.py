@@ -38,7 +38,7 @@ class MoPair(ctypes.Structure):
 
 
 class MoDfOptions(ctypes.Structure):
-    _fields_ = [("method", ctypes.c_int32), ("packet", ctypes.c_int32)]
+    _fields_ = [("method", ctypes.c_int32), ("packet", ctypes.c_int32), ("band", _F), ("reserved", ctypes.c_int32)]
 
 
 class MoTile(ctypes.Structure):
@@ -58,7 +58,8 @@ class MoRequest(ctypes.Structure):
                 ("nv", _I64), ("nf", _I64), ("ntv", _I64), ("ntf", _I64),
                 ("inputs_on_host", ctypes.c_int32), ("N", ctypes.c_int32), ("steps", ctypes.c_int32),
                 ("w_edge", _F), ("lr", ctypes.c_double), ("layout", ctypes.c_int32),
-                ("slices_per_tile", ctypes.c_int32), ("df_method", ctypes.c_int32), ("df_packet", ctypes.c_int32)]
+                ("slices_per_tile", ctypes.c_int32), ("df_method", ctypes.c_int32), ("df_packet", ctypes.c_int32),
+                ("df_band", _F), ("reserved", ctypes.c_int32)]
 
 
 class MoPoolStats(ctypes.Structure):
@@ -79,6 +80,7 @@ _SIGS = {
     "mo_df_build_scratch_bytes": (_SZ, [_I64, _I64, _I, _I]),
     "mo_df_build": (_I, [_P, _I64, _P, _I64, _I, _P, _I, _P, _SZ, _P, _P, _P]),
     "mo_df_method_for": (_I, [_I64, _I]),
+    "mo_df_loss_band": (_F, [_I]),
     "mo_df_build_ex": (_I, [_P, _I64, _P, _I64, _I, _P, _P, _P, _SZ, _P, _P, _P]),
     "mo_df_build_noalloc": (_I, [_P, _I64, _P, _I64, _I, _P, _P, _P]),
     "mo_df_noalloc_scratch_capacity": (_SZ, []),
@@ -123,6 +125,7 @@ _SIGS = {
     "mo_pool_run_groups": (_I, [_P, _I]),
     "mo_pool_group_time": (_I, [_P, _P, _P]),
     "mo_pool_stats": (_I, [_P, _P]),
+    "mo_pool_trim": (_I, [_P, ctypes.c_uint64]),
     "mo_pool_step_stream": (_I, [_P, _P]),
 }
 

@@ -2,7 +2,8 @@
 
 * distance-field build: method (shared-memory brute force or LBVH) and the
   LBVH traversal packet shape (the 32 voxels a warp walks the tree with:
-  4x4x2, 8x4x1, 4x2x4, 2x4x4, 8x2x2);
+  4x4x2, 8x4x1, 4x2x4, 2x4x4, 8x2x2), timed with the loss-preserving band
+  the serving builds use;
 * fused-step configuration: grid brick layout (linear [z][y][x], 2x2x2
   overlapping cell bricks of 32 B, or 4x4x4 bricks of 256 B) and tile width
   (32-vertex slices per tile, 1-8).
@@ -121,12 +122,13 @@ class Autotuner:
         grid = torch.empty(N ** 3, dtype=torch.float32, device=dev)
         nb = max(lib.mo_df_build_scratch_bytes(Vd.shape[0], Fd.shape[0], N, m) for m in (L.MO_DF_BRUTE, L.MO_DF_LBVH))
         scratch = torch.empty(int(nb), dtype=torch.uint8, device=dev)
+        band = lib.mo_df_loss_band(N)  # the serving builds' band
         cands = [(L.MO_DF_LBVH, p) for p in PACKETS.values()]
         if Fd.shape[0] * float(N) ** 3 <= 2e9:
             cands.append((L.MO_DF_BRUTE, L.MO_PACKET_4x4x2))
         results = {}
         for method, packet in cands:
-            opt = L.MoDfOptions(method, packet)
+            opt = L.MoDfOptions(method, packet, band)
 
             def run(opt=opt):
                 call("mo_df_build_ex", ptr(Vd), Vd.shape[0], ptr(Fd), Fd.shape[0], N, ptr(prm),

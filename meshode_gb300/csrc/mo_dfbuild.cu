@@ -6,6 +6,8 @@
 // igl::point_mesh_squared_distance query (mesh.cc:140) returns the exact
 // squared distance to the nearest triangle; the grid stores its sqrt.
 #include <cfloat>
+#include <cmath>
+#include <cstring>
 #include <mutex>
 
 #include "mo_common.cuh"
@@ -379,10 +381,16 @@ __device__ __forceinline__ float box_d2(float px, float py, float pz, float4 lo,
 
 // Packet shapes (voxels per warp along x, y, z; product 32), selectable per
 // launch: MO_PACKET_4x4x2 (default), 8x4x1, 4x2x4, 2x4x4, 8x2x2.
+// Band: with band > 0 a voxel whose distance is not below `band` stores
+// `band` itself, except in the two lowest layers along each axis (x, y or
+// z <= 1), which stay exact everywhere; band2 = band^2 (FLT_MAX for none).
+__device__ __forceinline__ bool exact_layer(int x, int y, int z) { return x <= 1 || y <= 1 || z <= 1; }
+
 template <int PX, int PY, int PZ>
 __global__ void __launch_bounds__(TRAV_WARPS * 32) k_df_lbvh(const float4* __restrict__ nodes,
                                                              const float4* __restrict__ tris, int ntri, int N,
-                                                             float* __restrict__ grid, int* __restrict__ status) {
+                                                             float band, float band2, float* __restrict__ grid,
+                                                             int* __restrict__ status) {
     __shared__ int stack[TRAV_WARPS][TRAV_STACK];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     static_assert(PX * PY * PZ == 32, "a packet is one warp");
@@ -394,17 +402,20 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) k_df_lbvh(const float4* __res
     const bool valid = x < N && y < N && z < N;
     const float Nf = (float)N;
     const float px = __fdiv_rn((float)x, Nf), py = __fdiv_rn((float)y, Nf), pz = __fdiv_rn((float)z, Nf);
-    float best = valid ? FLT_MAX : -1.0f;
+    const float init = exact_layer(x, y, z) ? FLT_MAX : band2;
+    float best = valid ? init : -1.0f;
     // Boxes are visited while their fp32 distance is within kSlack (in
     // distance units) of the lane's best: the rounding of the box bound can
     // exceed a triangle's computed distance by far less than that, so no
     // triangle that could lower `best` is skipped and the result is the exact
-    // minimum of the computed distances, whatever the visit order.
-    float lim = valid ? FLT_MAX : -1.0f;
+    // minimum of the computed distances, whatever the visit order.  Starting
+    // from band^2 instead of FLT_MAX skips what lies beyond the band and keeps
+    // every distance below it.
+    float lim = valid ? (init == FLT_MAX ? FLT_MAX : slack_bound(init)) : -1.0f;
     const unsigned FULL = 0xffffffffu;
     if (ntri == 1) {
         const float t = tri_d2(px, py, pz, load_tri(tris, 0), best);
-        if (valid) best = t;
+        if (valid && t < best) best = t;
     } else {
         int sp = 0;
         int node = 0;
@@ -455,25 +466,26 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) k_df_lbvh(const float4* __res
             __syncwarp();
         }
     }
-    if (valid) grid[((int64_t)z * N + y) * N + x] = __fsqrt_rn(best);
+    if (valid) grid[((int64_t)z * N + y) * N + x] = best < band2 || init == FLT_MAX ? __fsqrt_rn(best) : band;
 }
 
 template <int PX, int PY, int PZ>
-static void launch_df_lbvh_shape(const float4* nodes, const float4* tris, int ntri, int N, float* grid, int* status,
-                                 cudaStream_t s) {
+static void launch_df_lbvh_shape(const float4* nodes, const float4* tris, int ntri, int N, float band, float band2,
+                                 float* grid, int* status, cudaStream_t s) {
     const int64_t bricks = (int64_t)((N + PX - 1) / PX) * ((N + PY - 1) / PY) * ((N + PZ - 1) / PZ);
-    k_df_lbvh<PX, PY, PZ><<<ceil_div(bricks, TRAV_WARPS), TRAV_WARPS * 32, 0, s>>>(nodes, tris, ntri, N, grid, status);
+    k_df_lbvh<PX, PY, PZ><<<ceil_div(bricks, TRAV_WARPS), TRAV_WARPS * 32, 0, s>>>(nodes, tris, ntri, N, band, band2,
+                                                                                 grid, status);
     ::mo::note_launch();
 }
 
-static void launch_df_lbvh(int packet, const float4* nodes, const float4* tris, int ntri, int N, float* grid,
-                           int* status, cudaStream_t s) {
+static void launch_df_lbvh(int packet, const float4* nodes, const float4* tris, int ntri, int N, float band,
+                           float band2, float* grid, int* status, cudaStream_t s) {
     switch (packet) {
-        case MO_PACKET_8x4x1: launch_df_lbvh_shape<8, 4, 1>(nodes, tris, ntri, N, grid, status, s); break;
-        case MO_PACKET_4x2x4: launch_df_lbvh_shape<4, 2, 4>(nodes, tris, ntri, N, grid, status, s); break;
-        case MO_PACKET_2x4x4: launch_df_lbvh_shape<2, 4, 4>(nodes, tris, ntri, N, grid, status, s); break;
-        case MO_PACKET_8x2x2: launch_df_lbvh_shape<8, 2, 2>(nodes, tris, ntri, N, grid, status, s); break;
-        default: launch_df_lbvh_shape<4, 4, 2>(nodes, tris, ntri, N, grid, status, s); break;
+        case MO_PACKET_8x4x1: launch_df_lbvh_shape<8, 4, 1>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
+        case MO_PACKET_4x2x4: launch_df_lbvh_shape<4, 2, 4>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
+        case MO_PACKET_2x4x4: launch_df_lbvh_shape<2, 4, 4>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
+        case MO_PACKET_8x2x2: launch_df_lbvh_shape<8, 2, 2>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
+        default: launch_df_lbvh_shape<4, 4, 2>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
     }
 }
 
@@ -481,7 +493,7 @@ static void launch_df_lbvh(int packet, const float4* nodes, const float4* tris, 
 constexpr int BF_THREADS = 256, BF_CHUNK = 128;
 
 __global__ void __launch_bounds__(BF_THREADS) k_df_brute(const float4* __restrict__ tris, int ntri, int N,
-                                                         float* __restrict__ grid) {
+                                                         float band, float band2, float* __restrict__ grid) {
     __shared__ float4 sh[BF_CHUNK * TRI_F4];
     const int64_t v = (int64_t)blockIdx.x * BF_THREADS + threadIdx.x;
     const int64_t nvox = (int64_t)N * N * N;
@@ -489,7 +501,8 @@ __global__ void __launch_bounds__(BF_THREADS) k_df_brute(const float4* __restric
     const int x = (int)(v % N), y = (int)((v / N) % N), z = (int)(v / ((int64_t)N * N));
     const float Nf = (float)N;
     const float px = __fdiv_rn((float)x, Nf), py = __fdiv_rn((float)y, Nf), pz = __fdiv_rn((float)z, Nf);
-    float best = FLT_MAX;
+    const float init = exact_layer(x, y, z) ? FLT_MAX : band2;
+    float best = init;
     for (int base = 0; base < ntri; base += BF_CHUNK) {
         const int cnt = min(BF_CHUNK, ntri - base);
         __syncthreads();
@@ -502,7 +515,7 @@ __global__ void __launch_bounds__(BF_THREADS) k_df_brute(const float4* __restric
             best = fminf(best, tri_d2(px, py, pz, T, valid ? best : -1.0f));
         }
     }
-    if (valid) grid[v] = __fsqrt_rn(best);
+    if (valid) grid[v] = best < band2 || init == FLT_MAX ? __fsqrt_rn(best) : band;
 }
 
 // ---------------------------------------------------------------------------
@@ -593,6 +606,11 @@ extern "C" int mo_normalize(float* V, int64_t n, const double* params4, int inve
     return MO_OK;
 }
 
+extern "C" float mo_df_loss_band(int N) {
+    if (N < 2) return 0.0f;
+    return (float)(0.2 + std::sqrt(3.0) / (double)N + 1e-3);
+}
+
 extern "C" int mo_df_method_for(int64_t nf, int N) {
     // Brute force tests every voxel against every triangle; below ~3e8 pair
     // tests it beats building and walking the tree.
@@ -611,7 +629,10 @@ extern "C" int mo_df_build_ex(const float* V, int64_t nv, const int32_t* F, int6
                               float* grid_out, int32_t* status_out, void* stream) {
     int method = opt ? opt->method : MO_DF_AUTO;
     const int packet = opt ? opt->packet : MO_PACKET_4x4x2;
+    const float band = opt ? opt->band : 0.0f;
     MO_CHECK_ARG(packet >= MO_PACKET_4x4x2 && packet <= MO_PACKET_8x2x2, "unknown packet shape %d", packet);
+    MO_CHECK_ARG(band >= 0.0f && band <= 4.0f, "band must be in [0, 4] (0: exact grid), got %g", (double)band);
+    const float band2 = band > 0.0f ? band * band : FLT_MAX;
     MO_CHECK_ARG(nv > 0 && nf > 0, "target mesh must have vertices and faces (nv=%lld nf=%lld)", (long long)nv,
                  (long long)nf);
     MO_CHECK_ARG(nf < ((int64_t)1 << 30) && nv < ((int64_t)1 << 31), "target mesh too large");
@@ -646,7 +667,8 @@ extern "C" int mo_df_build_ex(const float* V, int64_t nv, const int32_t* F, int6
             k_check_faces<<<ceil_div(nf, 256), 256, 0, s>>>(F, nf, nv, st); ::mo::note_launch();
             k_tri_records<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, nullptr, S.tris, nullptr); ::mo::note_launch();
             const int64_t nvox = (int64_t)N * N * N;
-            k_df_brute<<<ceil_div(nvox, BF_THREADS), BF_THREADS, 0, s>>>(S.tris, (int)nf, N, grid_out); ::mo::note_launch();
+            k_df_brute<<<ceil_div(nvox, BF_THREADS), BF_THREADS, 0, s>>>(S.tris, (int)nf, N, band, band2, grid_out);
+            ::mo::note_launch();
         } else {
             k_morton<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.codes_a, S.ids_a, st); ::mo::note_launch();
             e = radix_sort_pairs(S.codes_a, S.ids_a, S.codes_b, S.ids_b, (int)nf, 30, S.hist, s);
@@ -656,7 +678,7 @@ extern "C" int mo_df_build_ex(const float* V, int64_t nv, const int32_t* F, int6
                 k_karras<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.codes_a, (int)nf, S.nodes, S.parent, S.flags); ::mo::note_launch();
                 k_refit<<<ceil_div(nf, 256), 256, 0, s>>>(S.boxes, (int)nf, S.nodes, S.parent, S.flags, S.rootbox, st); ::mo::note_launch();
             }
-            launch_df_lbvh(packet, S.nodes, S.tris, (int)nf, N, grid_out, st, s);
+            launch_df_lbvh(packet, S.nodes, S.tris, (int)nf, N, band, band2, grid_out, st, s);
         }
         e = cudaGetLastError();
         if (e != cudaSuccess) { fail(e, "df build kernels"); break; }
@@ -678,6 +700,7 @@ extern "C" int mo_df_build(const float* V, int64_t nv, const int32_t* F, int64_t
                            int method, void* scratch, size_t scratch_bytes, float* grid_out, int32_t* status_out,
                            void* stream) {
     MoDfOptions opt;
+    std::memset(&opt, 0, sizeof(opt));
     opt.method = method;
     opt.packet = MO_PACKET_4x4x2;
     return mo_df_build_ex(V, nv, F, nf, N, params4, &opt, scratch, scratch_bytes, grid_out, status_out, stream);

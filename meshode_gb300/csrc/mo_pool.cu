@@ -53,6 +53,7 @@ struct Req {
     int spt = MO_TILE_WARPS;
     int method = MO_DF_AUTO;
     int packet = MO_PACKET_4x4x2;
+    float band = 0.0f;
     int nslices = 0;
     int ntiles = 0;
     int t = 0;
@@ -217,8 +218,10 @@ int phase_a(MoPool* P, Req* R) {
     if (rc) return rc;
     const int N = q.N;
     MoDfOptions opt;
+    std::memset(&opt, 0, sizeof(opt));
     opt.method = R->method;
     opt.packet = R->packet;
+    opt.band = R->band;
     const size_t sb = mo_df_build_scratch_bytes(q.ntv, q.ntf, N, R->method);
     void* scratch = nullptr;
     float* glin = nullptr;
@@ -661,6 +664,8 @@ extern "C" int mo_pool_submit(MoPool* P, const MoRequest* q, int64_t* id_out) {
                  q->df_packet);
     R->method = q->df_method == MO_DF_AUTO ? mo_df_method_for(q->ntf, q->N) : q->df_method;
     R->packet = q->df_packet;
+    MO_CHECK_ARG(q->df_band <= 4.0f && q->df_band == q->df_band, "bad DF band %g", (double)q->df_band);
+    R->band = q->df_band < 0.0f ? mo_df_loss_band(q->N) : q->df_band;
     int rc = adam_table(P, q->lr, q->steps, &R->adam_tab);
     if (rc) return rc;
     R->id = P->next_id++;
@@ -812,6 +817,14 @@ extern "C" int mo_pool_group_time(MoPool* P, double* ms_out, double* bytes_out) 
 extern "C" int mo_pool_stats(MoPool* P, MoPoolStats* out) {
     MO_CHECK_ARG(P && out, "null pointer");
     *out = P->stats;
+    return MO_OK;
+}
+
+extern "C" int mo_pool_trim(MoPool* P, uint64_t keep_bytes) {
+    MO_CHECK_ARG(P, "null pool");
+    PCHK(cudaStreamSynchronize(P->step));
+    for (cudaStream_t s : P->builds) PCHK(cudaStreamSynchronize(s));
+    PCHK(cudaMemPoolTrimTo(P->mempool, (size_t)keep_bytes));
     return MO_OK;
 }
 

@@ -20,7 +20,7 @@ from ._lib import check
 class NativePool:
     def __init__(self, device=None, hbm_budget_bytes=None, max_pairs=512, max_tiles=None, group_steps=25,
                  layout=L.MO_LAYOUT_CELL, use_graph=True, max_building=8, results_to_host=True, build_streams=2,
-                 slices_per_tile=L.MO_TILE_WARPS, autotuner=None):
+                 slices_per_tile=L.MO_TILE_WARPS, autotuner=None, df_band=-1.0):
         L.require_cuda()
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
         self.lib = L.lib()
@@ -32,6 +32,8 @@ class NativePool:
         self.S = int(group_steps)
         self.layout = int(layout)
         self.autotuner = autotuner
+        # DF band: < 0 the loss-preserving band of mo_df_loss_band, 0 exact
+        self.df_band = float(df_band)
         self.results_to_host = bool(results_to_host)
         self._h = ctypes.c_void_p()
         with torch.cuda.device(self.device):
@@ -51,6 +53,10 @@ class NativePool:
             self.close()
         except Exception:
             pass
+
+    def trim(self, keep_bytes=0):
+        """Give the device memory the pool keeps for reuse back to the device."""
+        check(self.lib.mo_pool_trim(self._h, int(keep_bytes)), "mo_pool_trim")
 
     def stats(self):
         st = L.MoPoolStats()
@@ -86,7 +92,8 @@ class NativePool:
             srcV=tensors[0].data_ptr(), srcF=tensors[1].data_ptr(), tarV=tensors[2].data_ptr(),
             tarF=tensors[3].data_ptr(), nv=tensors[0].shape[0], nf=tensors[1].shape[0], ntv=tensors[2].shape[0],
             ntf=tensors[3].shape[0], inputs_on_host=0 if on_dev[0] else 1, N=r.N, steps=r.steps,
-            w_edge=r.w_edge, lr=r.lr, layout=layout, slices_per_tile=spt, df_method=method, df_packet=packet)
+            w_edge=r.w_edge, lr=r.lr, layout=layout, slices_per_tile=spt, df_method=method, df_packet=packet,
+            df_band=self.df_band)
         return q, tensors
 
     def _submit(self, r):

@@ -92,7 +92,7 @@ class _Job:
 class ServingEngine:
     def __init__(self, device=None, hbm_budget_bytes=None, max_pairs=512, max_tiles=None, group_steps=25,
                  layout=L.MO_LAYOUT_CELL, use_graph=True, max_building=8, results_to_host=True, lr=1e-3,
-                 build_streams=2, autotuner=None):
+                 build_streams=2, autotuner=None, df_band=-1.0):
         L.require_cuda()
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
         free, total = torch.cuda.mem_get_info(self.device)
@@ -111,6 +111,8 @@ class ServingEngine:
         self.max_building = int(max_building)
         # per-request DF build options and step layout / tile width
         self.autotuner = autotuner
+        # DF band: < 0 the loss-preserving band of mo_df_loss_band, 0 exact
+        self.df_band = float(df_band)
         self.results_to_host = bool(results_to_host)
         self.in_use = 0
         self.peak_in_use = 0
@@ -152,7 +154,8 @@ class ServingEngine:
             else:
                 method, packet = L.MO_DF_AUTO, L.MO_PACKET_4x4x2
                 job.layout, job.spt = self.layout, fused.SLICES_PER_TILE
-            opt = L.MoDfOptions(method, packet)
+            band = lib.mo_df_loss_band(N) if self.df_band < 0 else self.df_band
+            opt = L.MoDfOptions(method, packet, band)
             nb = lib.mo_df_build_scratch_bytes(Td.shape[0], TFd.shape[0], N, method)
             scratch = torch.empty(int(nb), dtype=torch.uint8, device=self.device)
             glin = torch.empty(N ** 3, dtype=torch.float32, device=self.device)

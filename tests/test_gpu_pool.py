@@ -1,6 +1,7 @@
 """The native serving pool (mo_pool_* in libmeshode.so) on the GPU.
 
-* Results are bit-identical to the Python serving engine's, to each request
+* Results (DF built with the loss-preserving band) are bit-identical to the
+  Python serving engine's on exact grids, to each request
   run alone, to the single-pair fused loop over the GPU pyDeform, with and
   without CUDA graphs, under Poisson pacing, and under a tile budget that
   forces requests to wait for room.
@@ -33,7 +34,8 @@ def test_pool_matches_python_engine_alone_and_paced(cuda):
     specs, meshes = _stream()
     base = serving.requests_from_meshes(meshes, specs, device=None, pin=True)
     ref = _fresh(base)
-    serving.ServingEngine(group_steps=8, max_building=3).run(ref)
+    # the Python engine on exact grids; the pool on the loss-preserving band
+    serving.ServingEngine(group_steps=8, max_building=3, df_band=0.0).run(ref)
     P = pool.NativePool(group_steps=8, max_building=3)
     mix = _fresh(base)
     P.run(mix)
