@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--cpu-sample-s", type=float, default=20.0)
     ap.add_argument("--no-extras", action="store_true", help="skip latency/plain/cpu legs")
     ap.add_argument("--no-autotune", action="store_true", help="fixed kernel choices instead of tuned ones")
+    ap.add_argument("--build-streams", type=int, default=2)
+    ap.add_argument("--max-building", type=int, default=8)
     ap.add_argument("--engine", default="native", choices=["native", "python"],
                     help="serving loop: the C++ pool behind mo_pool_* or the Python engine")
     return ap.parse_args()
@@ -436,9 +438,11 @@ def ours_arm(args, world, rank):
     def make_engine(results_to_host, max_pairs=512):
         if args.engine == "native":
             return pool.NativePool(device=dev, group_steps=args.group_steps, results_to_host=results_to_host,
-                                   autotuner=tuner, max_pairs=max_pairs, hbm_budget_bytes=budget)
+                                   autotuner=tuner, max_pairs=max_pairs, hbm_budget_bytes=budget,
+                                   build_streams=args.build_streams, max_building=args.max_building)
         return serving.ServingEngine(device=dev, group_steps=args.group_steps, results_to_host=results_to_host,
-                                     autotuner=tuner, max_pairs=max_pairs, hbm_budget_bytes=budget)
+                                     autotuner=tuner, max_pairs=max_pairs, hbm_budget_bytes=budget,
+                                     build_streams=args.build_streams, max_building=args.max_building)
 
     def fused_launches(eng):
         if args.engine == "native":
@@ -575,6 +579,7 @@ def ours_arm(args, world, rank):
         "config": {"workload": WORKLOAD, "requests": args.requests, "req_steps": args.req_steps,
                    "group_steps": args.group_steps, "parallelism": "replicas" if world > 1 else "single",
                    "engine": "mo_pool (C ABI)" if args.engine == "native" else "python",
+                   "build_streams": args.build_streams, "max_building": args.max_building,
                    "l2": "inputs larger than L2 (~1.3 GB meshes, ~20 GB grids per stream)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "kernel": "k_fused_step", "achieved": achieved_ss, "peak": peak,

@@ -263,7 +263,7 @@ typedef struct MoTile {
 #define MO_TILE_WARPS 8
 int mo_fused_step(const MoPair* pairs, const MoTile* tiles, const int32_t* ntiles, int max_tiles,
                   int launch_index, float* tile_loss, int grid_ctas, void* stream);
-/* pair_loss[k*npairs + p] (double) = sum, in tile order, of the tile
+/* pair_loss[k*npairs + p] (double) = sum, in a fixed order, of the tile
  * partials of pair p (its MoPair tile0/ntiles range) for launches
  * k = 0..nlaunch-1: the layer loss 0.5*sum d^2 + w_edge*0.5*sum |r|^2 at the
  * positions before step t0+k+1. */

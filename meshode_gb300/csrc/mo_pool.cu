@@ -424,10 +424,15 @@ int run_group(MoPool* P) {
         P->group_events.push_back({e0, e1});
         P->group_bytes.push_back(bytes);
     }
-    // per-pair losses of this group's launches (a retiring pair keeps its last)
-    rc = mo_pair_loss(P->pairs_dev, n, P->cfg.max_tiles, P->cfg.group_steps, P->tile_loss, P->pair_loss,
-                      reinterpret_cast<void*>(P->step));
-    if (rc) return rc;
+    // per-pair losses of this group's launches, when a pair retires (it keeps
+    // the loss of its last step)
+    bool retire = false;
+    for (int64_t id : P->active) retire |= P->reqs[id]->t + P->cfg.group_steps >= P->reqs[id]->in.steps;
+    if (retire) {
+        rc = mo_pair_loss(P->pairs_dev, n, P->cfg.max_tiles, P->cfg.group_steps, P->tile_loss, P->pair_loss,
+                          reinterpret_cast<void*>(P->step));
+        if (rc) return rc;
+    }
     P->stats.groups += 1;
     std::vector<int64_t> still;
     still.reserve(n);

@@ -159,17 +159,24 @@ __global__ void __launch_bounds__(STEP_THREADS, 4) k_fused_step(const MoPair* __
     }
 }
 
-__global__ void k_pair_loss(const MoPair* __restrict__ pairs, int npairs, int max_tiles, int nlaunch,
-                            const float* __restrict__ tile_loss, double* __restrict__ out) {
-    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= (int64_t)npairs * nlaunch) return;
+// One warp per (pair, launch): lane l sums the pair's tile partials l, l+32,
+// ... in double, then a fixed shuffle tree adds the 32 lane sums.  The order
+// is fixed, so the result does not depend on scheduling.
+__global__ void __launch_bounds__(128) k_pair_loss(const MoPair* __restrict__ pairs, int npairs, int max_tiles,
+                                                   int nlaunch, const float* __restrict__ tile_loss,
+                                                   double* __restrict__ out) {
+    const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (q >= (int64_t)npairs * nlaunch) return;  // warp-uniform
     const int p = (int)(q % npairs), k = (int)(q / npairs);
     const MoPair& P = pairs[p];
-    double s = 0.0;
     const float* base = tile_loss + (int64_t)k * max_tiles * TILE_WARPS;
-    for (int64_t t = (int64_t)P.tile0 * TILE_WARPS; t < (int64_t)(P.tile0 + P.ntiles) * TILE_WARPS; ++t)
-        s += (double)base[t];
-    out[(int64_t)k * npairs + p] = s;
+    const int64_t t0 = (int64_t)P.tile0 * TILE_WARPS, t1 = (int64_t)(P.tile0 + P.ntiles) * TILE_WARPS;
+    double s = 0.0;
+    for (int64_t t = t0 + lane; t < t1; t += 32) s += (double)base[t];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) out[(int64_t)k * npairs + p] = s;
 }
 
 __global__ void k_pack(const float* __restrict__ V, int64_t n, float4* __restrict__ out) {
@@ -232,8 +239,8 @@ extern "C" int mo_pair_loss(const MoPair* pairs, int npairs, int max_tiles, int 
     const int64_t n = (int64_t)npairs * nlaunch;
     if (n == 0) return MO_OK;
     MO_CHECK_ARG(pairs && tile_loss && pair_loss, "null pointer");
-    k_pair_loss<<<ceil_div(n, 128), 128, 0, as_stream(stream)>>>(pairs, npairs, max_tiles, nlaunch, tile_loss,
-                                                                pair_loss); ::mo::note_launch();
+    k_pair_loss<<<ceil_div(n, 4), 128, 0, as_stream(stream)>>>(pairs, npairs, max_tiles, nlaunch, tile_loss,
+                                                              pair_loss); ::mo::note_launch();
     MO_LAUNCH_CHECK("k_pair_loss");
     return MO_OK;
 }

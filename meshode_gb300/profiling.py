@@ -4,12 +4,14 @@
         the first `pairs` requests of the serving stream prepared and stepped
         together: `groups` x 25 launches of k_fused_step with every pair
         active (plus one warm-up group);
-    python -m meshode_gb300.profiling df --request 1 --repeat 2
-        the distance-field build of one request of the stream, `repeat` times.
+    python -m meshode_gb300.profiling df --request 1 --repeat 2 [--band] [--packet 4x2x4]
+        the distance-field build of one request of the stream, `repeat` times
+        (--band: with the loss-preserving band the serving builds use).
 
 Each prints one line with the CUDA-event timing of the measured launches.
 """
 import argparse
+import ctypes
 import sys
 
 import torch
@@ -17,7 +19,6 @@ import torch
 from . import _lib as L
 from . import build as B
 from . import meshgen, serving
-from . import pyDeform as PD
 
 
 def _stream(n, seed=5):
@@ -46,18 +47,32 @@ def df(args):
     Vd = torch.from_numpy(Vt).to(dev)
     Fd = torch.from_numpy(Ft).to(dev)
     method = {"auto": L.MO_DF_AUTO, "brute": L.MO_DF_BRUTE, "lbvh": L.MO_DF_LBVH}[args.method]
+    from . import autotune
+    N = s["N"]
+    lib = L.lib()
+    band = lib.mo_df_loss_band(N) if args.band else 0.0
+    opt = L.MoDfOptions(method, autotune.PACKETS[args.packet], band)
+    st = L.stream_ptr()
+    bbox = torch.empty(6, dtype=torch.int32, device=dev)
+    prm = torch.empty(4, dtype=torch.float64, device=dev)
+    L.call("mo_bbox", L.ptr(Vd), Vd.shape[0], L.ptr(bbox), st)
+    L.call("mo_norm_params", L.ptr(bbox), L.ptr(prm), st)
+    nb = lib.mo_df_build_scratch_bytes(Vd.shape[0], Fd.shape[0], N, method)
+    scratch = torch.empty(int(nb), dtype=torch.uint8, device=dev)
+    grid = torch.empty(N ** 3, dtype=torch.float32, device=dev)
     times = []
     for _ in range(args.repeat):
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()
-        PD.InitializeDeformTemplate(Vd, Fd, 0, s["N"], df_method=method)
+        L.call("mo_df_build_ex", L.ptr(Vd), Vd.shape[0], L.ptr(Fd), Fd.shape[0], N, L.ptr(prm),
+               ctypes.byref(opt), L.ptr(scratch), nb, L.ptr(grid), None, st)
         e1.record()
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1))
-    print("df build: request %d, N=%d, %d triangles, ms per build %s"
-          % (args.request, s["N"], Ft.shape[0], ", ".join("%.2f" % t for t in times)))
+    print("df build: request %d, N=%d, %d triangles, band %.4f, packet %s, ms per build %s"
+          % (args.request, N, Ft.shape[0], band, args.packet, ", ".join("%.2f" % t for t in times)))
 
 
 def main(argv=None):
@@ -70,6 +85,8 @@ def main(argv=None):
     b.add_argument("--request", type=int, default=1)
     b.add_argument("--repeat", type=int, default=2)
     b.add_argument("--method", default="auto", choices=["auto", "brute", "lbvh"])
+    b.add_argument("--band", action="store_true")
+    b.add_argument("--packet", default="4x4x2", choices=["4x4x2", "8x4x1", "4x2x4", "2x4x4", "8x2x2"])
     args = ap.parse_args(argv)
     B.build()
     L.require_cuda()
