@@ -62,8 +62,8 @@ def parse():
     ap.add_argument("--cpu-sample-s", type=float, default=20.0)
     ap.add_argument("--no-extras", action="store_true", help="skip latency/plain/cpu legs")
     ap.add_argument("--no-autotune", action="store_true", help="fixed kernel choices instead of tuned ones")
-    ap.add_argument("--build-streams", type=int, default=2)
-    ap.add_argument("--max-building", type=int, default=8)
+    ap.add_argument("--build-streams", type=int, default=6)
+    ap.add_argument("--max-building", type=int, default=16)
     ap.add_argument("--engine", default="native", choices=["native", "python"],
                     help="serving loop: the C++ pool behind mo_pool_* or the Python engine")
     return ap.parse_args()

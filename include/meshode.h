@@ -315,7 +315,9 @@ typedef struct MoRequest {
     int32_t df_method;      /* MO_DF_AUTO / BRUTE / LBVH */
     int32_t df_packet;      /* MO_PACKET_* */
     float df_band;          /* < 0: mo_df_loss_band(N); 0: exact grid; > 0: this band */
-    int32_t reserved;       /* 0 */
+    int32_t out_on_host;    /* V_out is host memory (pinned, for the copy to overlap) */
+    float* V_out;           /* optional [nv,3]: the denormalised result, written at retirement */
+    float* V_normalized_out;/* optional device [nv,3]: the result in the target-normalised frame */
 } MoRequest;
 
 #define MO_REQ_FAILED (-1)
@@ -338,8 +340,10 @@ typedef struct MoPoolStats {
 int mo_pool_create(const MoPoolConfig* cfg, MoPool** pool_out);
 int mo_pool_destroy(MoPool* pool);
 /* Queue a request.  The input arrays must stay valid and unchanged until the
- * request is finished (DONE or FAILED).  Checks sizes and options on the host;
- * invalid meshes (a face index out of range) fail the request later. */
+ * request is finished (DONE or FAILED), and so must the optional output
+ * arrays, which the pool fills on its step stream as the request retires
+ * (complete once the request is DONE).  Checks sizes and options on the
+ * host; invalid meshes (a face index out of range) fail the request later. */
 int mo_pool_submit(MoPool* pool, const MoRequest* req, int64_t* id_out);
 /* Admit, advance builds, run one group over the active pairs, collect
  * retirements.  block != 0: when nothing is active, wait for the oldest build

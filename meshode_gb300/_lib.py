@@ -59,7 +59,7 @@ class MoRequest(ctypes.Structure):
                 ("inputs_on_host", ctypes.c_int32), ("N", ctypes.c_int32), ("steps", ctypes.c_int32),
                 ("w_edge", _F), ("lr", ctypes.c_double), ("layout", ctypes.c_int32),
                 ("slices_per_tile", ctypes.c_int32), ("df_method", ctypes.c_int32), ("df_packet", ctypes.c_int32),
-                ("df_band", _F), ("reserved", ctypes.c_int32)]
+                ("df_band", _F), ("out_on_host", ctypes.c_int32), ("V_out", _P), ("V_normalized_out", _P)]
 
 
 class MoPoolStats(ctypes.Structure):

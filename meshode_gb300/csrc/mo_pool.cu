@@ -454,6 +454,10 @@ int run_group(MoPool* P) {
         PCHK(cudaMemcpyAsync(denorm, normed, 12 * nv, cudaMemcpyDeviceToDevice, P->step));
         rc = mo_normalize(denorm, nv, R->params, 1, sv);
         if (rc) return rc;
+        const cudaMemcpyKind ok = R->in.out_on_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+        if (R->in.V_out) PCHK(cudaMemcpyAsync(R->in.V_out, denorm, 12 * nv, ok, P->step));
+        if (R->in.V_normalized_out)
+            PCHK(cudaMemcpyAsync(R->in.V_normalized_out, normed, 12 * nv, cudaMemcpyDeviceToDevice, P->step));
         PCHK(cudaMemcpyAsync(&R->host->loss, P->pair_loss + (int64_t)(k - 1) * n + i, 8, cudaMemcpyDeviceToHost,
                              P->step));
         PCHK(cudaEventRecord(R->ev, P->step));
@@ -759,7 +763,7 @@ extern "C" int mo_pool_result(MoPool* P, int64_t id, float* V_out, float* V_norm
     // for just these copies, so the result memory can be recycled afterwards
     if (V_out) PCHK(cudaMemcpyAsync(V_out, R->result + 3 * R->in.nv, bytes, kind, P->io));
     if (V_normalized_out) PCHK(cudaMemcpyAsync(V_normalized_out, R->result, bytes, kind, P->io));
-    PCHK(cudaStreamSynchronize(P->io));
+    if (V_out || V_normalized_out) PCHK(cudaStreamSynchronize(P->io));
     if (loss_out) *loss_out = R->host->loss;
     return MO_OK;
 }

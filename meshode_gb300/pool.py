@@ -19,7 +19,7 @@ from ._lib import check
 
 class NativePool:
     def __init__(self, device=None, hbm_budget_bytes=None, max_pairs=512, max_tiles=None, group_steps=25,
-                 layout=L.MO_LAYOUT_CELL, use_graph=True, max_building=8, results_to_host=True, build_streams=2,
+                 layout=L.MO_LAYOUT_CELL, use_graph=True, max_building=16, results_to_host=True, build_streams=6,
                  slices_per_tile=L.MO_TILE_WARPS, autotuner=None, df_band=-1.0):
         L.require_cuda()
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
@@ -88,56 +88,49 @@ class NativePool:
         if self.autotuner is not None:
             method, packet = self.autotuner.df_options(r.N, int(tensors[3].shape[0]))
             layout, spt = self.autotuner.step_options(r.N, int(tensors[0].shape[0]))
+        # result buffers the pool fills as the request retires
+        nv = int(tensors[0].shape[0])
+        if self.results_to_host:
+            out = torch.empty(nv, 3, dtype=torch.float32).pin_memory()
+        else:
+            out = torch.empty(nv, 3, dtype=torch.float32, device=self.device)
+        normed = torch.empty(nv, 3, dtype=torch.float32, device=self.device)
         q = L.MoRequest(
             srcV=tensors[0].data_ptr(), srcF=tensors[1].data_ptr(), tarV=tensors[2].data_ptr(),
-            tarF=tensors[3].data_ptr(), nv=tensors[0].shape[0], nf=tensors[1].shape[0], ntv=tensors[2].shape[0],
+            tarF=tensors[3].data_ptr(), nv=nv, nf=tensors[1].shape[0], ntv=tensors[2].shape[0],
             ntf=tensors[3].shape[0], inputs_on_host=0 if on_dev[0] else 1, N=r.N, steps=r.steps,
             w_edge=r.w_edge, lr=r.lr, layout=layout, slices_per_tile=spt, df_method=method, df_packet=packet,
-            df_band=self.df_band)
-        return q, tensors
+            df_band=self.df_band, out_on_host=1 if self.results_to_host else 0, V_out=out.data_ptr(),
+            V_normalized_out=normed.data_ptr())
+        return q, tensors + [out, normed]
 
     def _submit(self, r):
-        q, tensors = self._request(r)
+        q, keep = self._request(r)
         rid = ctypes.c_int64()
         check(self.lib.mo_pool_submit(self._h, ctypes.byref(q), ctypes.byref(rid)), "mo_pool_submit")
-        self._keep[rid.value] = (r, tensors)
+        self._keep[rid.value] = (r, keep)
         return rid.value
 
     def _collect(self):
         ids = (ctypes.c_int64 * 64)()
         n = ctypes.c_int()
+        st = ctypes.c_int32()
+        loss = ctypes.c_double()
         done = 0
         while True:
             check(self.lib.mo_pool_completed(self._h, ids, 64, ctypes.byref(n)), "mo_pool_completed")
-            if n.value:
-                # the results are written from the pool's I/O stream into memory
-                # torch's stream may have used a moment ago
-                torch.cuda.current_stream(self.device).synchronize()
             for k in range(n.value):
                 pid = ids[k]
-                r, _ = self._keep.pop(pid)
-                st = ctypes.c_int32()
+                r, keep = self._keep.pop(pid)
                 check(self.lib.mo_pool_state(self._h, pid, ctypes.byref(st)), "mo_pool_state")
                 if st.value == L.MO_REQ_FAILED:
                     buf = ctypes.create_string_buffer(256)
                     self.lib.mo_pool_error(self._h, pid, buf, 256)
                     r.error = buf.value.decode()
                 else:
-                    nv = int(r.srcV.shape[0])
-                    normed = torch.empty(nv, 3, dtype=torch.float32, device=self.device)
-                    loss = ctypes.c_double()
-                    if self.results_to_host:
-                        out = torch.empty(nv, 3, dtype=torch.float32).pin_memory()
-                        # out_on_host applies to both outputs of one call: two calls
-                        check(self.lib.mo_pool_result(self._h, pid, None, ctypes.c_void_p(normed.data_ptr()), 0,
-                                                      None), "mo_pool_result")
-                        check(self.lib.mo_pool_result(self._h, pid, ctypes.c_void_p(out.data_ptr()), None, 1,
-                                                      ctypes.byref(loss)), "mo_pool_result")
-                    else:
-                        out = torch.empty(nv, 3, dtype=torch.float32, device=self.device)
-                        check(self.lib.mo_pool_result(self._h, pid, ctypes.c_void_p(out.data_ptr()),
-                                                      ctypes.c_void_p(normed.data_ptr()), 0, ctypes.byref(loss)),
-                              "mo_pool_result")
+                    out, normed = keep[4], keep[5]
+                    check(self.lib.mo_pool_result(self._h, pid, None, None, 0, ctypes.byref(loss)),
+                          "mo_pool_result")
                     r.out = out
                     r.out_normalized = normed
                     r.loss = loss.value

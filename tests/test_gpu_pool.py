@@ -130,3 +130,50 @@ def test_pool_steady_state(cuda):
     assert t > 0 and nv == sum(int(r.srcV.shape[0]) for r in reqs)
     assert nbytes == sum(104 * int(r.srcV.shape[0]) + 44 * 3 * int(r.srcF.shape[0]) for r in reqs)
     P.close()
+
+
+def test_pool_c_abi_direct(cuda):
+    """The pool driven through the C ABI alone (as a C host would): host
+    inputs, no output buffers, mo_pool_wait, then mo_pool_result into host
+    arrays; equal to the facade's results."""
+    import ctypes
+    import numpy as np
+    from meshode_gb300 import _lib as L
+    specs, meshes = _stream(n=3, seed=17)
+    base = serving.requests_from_meshes(meshes, specs, device=None, pin=True)
+    ref = _fresh(base)
+    pool.NativePool(group_steps=9).run(ref)
+    lib = L.lib()
+    cfg = L.MoPoolConfig(max_pairs=8, max_tiles=4096, group_steps=9, use_graph=1, layout=L.MO_LAYOUT_CELL)
+    h = ctypes.c_void_p()
+    L.check(lib.mo_pool_create(ctypes.byref(cfg), ctypes.byref(h)), "create")
+    arrays = [[np.ascontiguousarray(a) for a in m] for m in meshes]
+    ids = []
+    for (Vs, Fs, Vt, Ft), r in zip(arrays, base):
+        q = L.MoRequest(srcV=Vs.ctypes.data, srcF=Fs.ctypes.data, tarV=Vt.ctypes.data, tarF=Ft.ctypes.data,
+                        nv=len(Vs), nf=len(Fs), ntv=len(Vt), ntf=len(Ft), inputs_on_host=1, N=r.N, steps=r.steps,
+                        w_edge=1.0, lr=1e-3, layout=-1, df_band=-1.0)
+        rid = ctypes.c_int64()
+        L.check(lib.mo_pool_submit(h, ctypes.byref(q), ctypes.byref(rid)), "submit")
+        ids.append(rid.value)
+    L.check(lib.mo_pool_wait(h), "wait")
+    st = L.MoPoolStats()
+    L.check(lib.mo_pool_stats(h, ctypes.byref(st)), "stats")
+    assert st.submitted == 3 and st.done == 3 and st.failed == 0 and st.active == 0 and st.fused_launches > 0
+    got = (ctypes.c_int64 * 8)()
+    n = ctypes.c_int()
+    L.check(lib.mo_pool_completed(h, got, 8, ctypes.byref(n)), "completed")
+    assert sorted(got[:n.value]) == sorted(ids)
+    for rid, r, (Vs, _, _, _) in zip(ids, ref, arrays):
+        out = np.empty_like(Vs)
+        loss = ctypes.c_double()
+        L.check(lib.mo_pool_result(h, rid, out.ctypes.data, None, 1, ctypes.byref(loss)), "result")
+        assert np.array_equal(out, r.out.numpy())
+        assert loss.value == r.loss
+        state = ctypes.c_int32()
+        L.check(lib.mo_pool_state(h, rid, ctypes.byref(state)), "state")
+        assert state.value == L.MO_REQ_DONE
+        L.check(lib.mo_pool_release(h, rid), "release")
+    assert lib.mo_pool_state(h, ids[0], ctypes.byref(state)) == L.MO_ERR_INVALID
+    L.check(lib.mo_pool_trim(h, 0), "trim")
+    L.check(lib.mo_pool_destroy(h), "destroy")
