@@ -381,6 +381,41 @@ int mo_pool_trim(MoPool* pool, uint64_t keep_bytes);
 /* The pool's step stream (a cudaStream_t). */
 int mo_pool_step_stream(MoPool* pool, void** stream_out);
 /* ------------------------------------------------------------------------
+ * Reverse (target -> source) nearest-point loss.  Replaces ReverseLossLayer
+ * (src/python/layers/reverse_loss_layer.py:14-25): ii = cKDTree(src_V)
+ * .query(tar_V, k=1); loss = 0.5 * sum |src_V[ii] - tar_V|^2, and its
+ * autograd backward.  Used per step by inverse_deform.py:26-31 and
+ * cad_deform2.py:46-52.
+ * ------------------------------------------------------------------------ */
+size_t mo_nn_scratch_bytes(int64_t np, int64_t nq);
+/* idx_out[q] (int32 [nq]) = the index of the point of P [np,3] nearest to
+ * Q[q] (squared Euclidean distance in double, summed x, y, z, as cKDTree
+ * computes it from float32 input; exact ties go to the lowest index);
+ * d2_out (optional, double [nq]) = that squared distance.  scratch NULL:
+ * allocated stream-ordered.  Synchronises `stream`; MO_ERR_DEVICE when a
+ * query is not finite or no point is. */
+int mo_nn_query(const float* P, int64_t np, const float* Q, int64_t nq, int32_t* idx_out, double* d2_out,
+                void* scratch, size_t scratch_bytes, void* stream);
+size_t mo_reverse_loss_scratch_bytes(int64_t ns, int64_t nt);
+/* loss_out (device double [1]) = 0.5 * sum over t of |src[idx[t]] - tar[t]|^2,
+ * the differences and squares in float like the reference's tensors, summed
+ * in double in a fixed order.  status_out: optional device int32; when given
+ * the call does not synchronise and bit 0 is OR-ed in for an index outside
+ * [0, ns) (that term skipped); when NULL the call synchronises and returns
+ * MO_ERR_DEVICE for it. */
+int mo_reverse_loss_forward(const float* src, int64_t ns, const float* tar, int64_t nt, const int32_t* idx,
+                            double* loss_out, void* scratch, size_t scratch_bytes, int32_t* status_out,
+                            void* stream);
+/* grad_src [ns,3] = the gradient of grad_out (device float [1]) * that loss
+ * with respect to src, bit-identical to torch's CPU autograd of the
+ * reference expression: per source vertex, over its matched targets in
+ * increasing t, the sum from zero of (g*l + g*l), l = src[i] - tar[t],
+ * g = 0.5 * grad_out.  status_out as above. */
+int mo_reverse_loss_backward(const float* src, int64_t ns, const float* tar, int64_t nt, const int32_t* idx,
+                             const float* grad_out, float* grad_src, void* scratch, size_t scratch_bytes,
+                             int32_t* status_out, void* stream);
+
+/* ------------------------------------------------------------------------
  * Velocity-field ODE deformation (the NeuralODE variant,
  * src/python/layers/neuralode_fast.py:7-64; here 3 -> m -> m -> m -> 3 with
  * softplus and fixed-step RK4).  The m x m layers are plain GEMMs done by

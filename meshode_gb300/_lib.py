@@ -110,6 +110,11 @@ _SIGS = {
     "mo_mlp_in_bwd": (_I, [_P, _I64, _I, _P, _P, _I, _P]),
     "mo_pack_pos": (_I, [_P, _I64, _P, _P]),
     "mo_unpack_pos": (_I, [_P, _I64, _P, _P]),
+    "mo_nn_scratch_bytes": (_SZ, [_I64, _I64]),
+    "mo_nn_query": (_I, [_P, _I64, _P, _I64, _P, _P, _P, _SZ, _P]),
+    "mo_reverse_loss_scratch_bytes": (_SZ, [_I64, _I64]),
+    "mo_reverse_loss_forward": (_I, [_P, _I64, _P, _I64, _P, _P, _P, _SZ, _P, _P]),
+    "mo_reverse_loss_backward": (_I, [_P, _I64, _P, _I64, _P, _P, _P, _P, _SZ, _P, _P]),
     "mo_pool_create": (_I, [_P, _P]),
     "mo_pool_destroy": (_I, [_P]),
     "mo_pool_submit": (_I, [_P, _P, _P]),

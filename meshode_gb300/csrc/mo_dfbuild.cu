@@ -11,6 +11,7 @@
 #include <mutex>
 
 #include "mo_common.cuh"
+#include "mo_lbvh.cuh"
 
 namespace mo {
 
@@ -213,22 +214,6 @@ __device__ __forceinline__ void store_tri(float4* __restrict__ tris, int i, cons
 // ---------------------------------------------------------------------------
 // Morton codes (identical float operations to the oracle's restatement).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t spread10(uint32_t x) {
-    x &= 0x3ffu;
-    x = (x | (x << 16)) & 0x030000ffu;
-    x = (x | (x << 8)) & 0x0300f00fu;
-    x = (x | (x << 4)) & 0x030c30c3u;
-    x = (x | (x << 2)) & 0x09249249u;
-    return x;
-}
-
-__device__ __forceinline__ uint32_t quant10(float c) {
-    float q = MUL(c, 1024.0f);
-    q = fmaxf(q, 0.0f);
-    q = fminf(q, 1023.0f);
-    return (uint32_t)q;
-}
-
 __global__ void k_morton(const float* __restrict__ Vn, const int32_t* __restrict__ F, int64_t nf, int64_t nv,
                          uint32_t* __restrict__ codes, int* __restrict__ ids, int* __restrict__ status) {
     const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;

@@ -94,3 +94,56 @@ class GraphLossLayer(nn.Module):
 
     def forward(self, src_V, src_E):
         return GraphLossFunction.apply(src_V, src_E, self.rigidity2, int(self.param_id))
+
+
+class ReverseLossFunction(Function):
+    """reverse_loss_layer.py:14-25: ii = nearest source vertex of every
+    target vertex (cKDTree in the reference, an LBVH query here), loss =
+    0.5 * sum |src_V[ii] - tar_V|^2.  The indices are constants of the
+    forward pass; the backward is torch's CPU autograd of that expression,
+    bit for bit.  The work runs on the GPU; the loss and the gradient come
+    back on src_V's device."""
+
+    @staticmethod
+    def forward(ctx, src_V, tar_V):
+        from . import _lib as L
+        L.require_cuda()
+        dev = torch.device("cuda", torch.cuda.current_device())
+        S = src_V.detach().to(dev, torch.float32).contiguous()
+        T = tar_V.detach().to(dev, torch.float32).contiguous()
+        if S.dim() != 2 or S.shape[1] != 3 or T.dim() != 2 or T.shape[1] != 3:
+            raise RuntimeError("ReverseLossLayer expects [n,3] source and target vertices")
+        ns, nt = int(S.shape[0]), int(T.shape[0])
+        s = L.stream_ptr()
+        idx = torch.empty(nt, dtype=torch.int32, device=dev)
+        L.call("mo_nn_query", L.ptr(S), ns, L.ptr(T), nt, L.ptr(idx), None, None, 0, s)
+        nb = L.lib().mo_reverse_loss_scratch_bytes(ns, nt)
+        scratch = torch.empty(max(int(nb), 1), dtype=torch.uint8, device=dev)
+        loss = torch.empty(1, dtype=torch.float64, device=dev)
+        L.call("mo_reverse_loss_forward", L.ptr(S), ns, L.ptr(T), nt, L.ptr(idx), L.ptr(loss), L.ptr(scratch), nb,
+               None, s)
+        ctx.save_for_backward(S, T, idx)
+        ctx.src_device = src_V.device
+        return loss.to(torch.float32).reshape(()).to(src_V.device)
+
+    @staticmethod
+    def backward(ctx, grad):
+        from . import _lib as L
+        S, T, idx = ctx.saved_tensors
+        ns, nt = int(S.shape[0]), int(T.shape[0])
+        g = grad.detach().to(S.device, torch.float32).reshape(1).contiguous()
+        gs = torch.empty_like(S)
+        nb = L.lib().mo_reverse_loss_scratch_bytes(ns, nt)
+        scratch = torch.empty(max(int(nb), 1), dtype=torch.uint8, device=S.device)
+        st = torch.zeros(1, dtype=torch.int32, device=S.device)  # the forward checked the indices
+        L.call("mo_reverse_loss_backward", L.ptr(S), ns, L.ptr(T), nt, L.ptr(idx), L.ptr(g), L.ptr(gs),
+               L.ptr(scratch), nb, L.ptr(st), L.stream_ptr())
+        return gs.to(ctx.src_device), None
+
+
+class ReverseLossLayer(nn.Module):
+    """reverse_loss_layer.py:10-25.  `device` is accepted for the reference's
+    signature; the result is on src_V's device."""
+
+    def forward(self, src_V, tar_V, device=None):
+        return ReverseLossFunction.apply(src_V, tar_V)

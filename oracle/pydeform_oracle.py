@@ -433,3 +433,18 @@ def graph_fit(src_V, src_E, pid, steps, rigidity2, lr=1e-3, adam="torch"):
             _, g = graph_loss_grad(V.data, src_E, pid, rigidity2)
             _adam_step(opt, V, g)
     return V.detach()
+
+
+def reverse_loss(src_V, tar_V):
+    """ReverseLossLayer.forward (src/python/layers/reverse_loss_layer.py:14-25)
+    on the CPU: cKDTree 1-NN of every target vertex among the source
+    vertices, then 0.5 * sum |src_V[ii] - tar_V|^2 with torch autograd.
+    (The reference passes n_jobs=4, which SciPy no longer accepts; the
+    neighbours do not depend on the thread count.)  Returns (loss, ii)."""
+    from scipy.spatial import cKDTree
+    tree = cKDTree(src_V.detach().cpu().numpy())
+    _, ii = tree.query(tar_V.detach().cpu().numpy(), k=1)
+    src_c = src_V[torch.from_numpy(ii)]
+    loss = src_c - tar_V
+    loss = 0.5 * (loss * loss).sum()
+    return loss, ii

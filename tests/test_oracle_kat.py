@@ -223,3 +223,15 @@ def test_exact_adam_definition_and_torch(orc):
         opt.step()
     diff = np.abs(Ve.detach().numpy() - Vt.detach().numpy()).max()
     assert diff <= 1e-6, diff
+
+
+def test_reverse_loss_known_answer(orc):
+    """Two source points, two targets: each target's nearest source point and
+    the loss 0.5*sum of squared offsets, with its autograd gradient."""
+    src = torch.tensor([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0]], requires_grad=True)
+    tar = torch.tensor([[0.875, 0.0, 0.0], [0.25, 0.0, 0.0], [0.75, 0.5, 0.0]])
+    loss, ii = orc.reverse_loss(src, tar)
+    assert list(ii) == [1, 0, 1]
+    assert float(loss) == pytest.approx(0.5 * (0.125 ** 2 + 0.25 ** 2 + 0.25 ** 2 + 0.5 ** 2))
+    loss.backward()
+    assert torch.equal(src.grad, torch.tensor([[-0.25, 0.0, 0.0], [0.125 + 0.25, -0.5, 0.0]]))
