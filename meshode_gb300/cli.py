@@ -4,6 +4,7 @@
         [GRID_RESOLUTION=64] [MESH_RESOLUTION=5000] [lambda=1] [symmetry=0]
     python -m meshode_gb300.cli cad_deform cad.obj reference.obj output.obj \\
         [GRID_RESOLUTION=64] [MESH_RESOLUTION=5000] [lambda=1] [symmetry=0] [flow_output]
+    python -m meshode_gb300.cli inverse_deform source.obj reference.obj output.obj
 
 Positional arguments, defaults and their order follow src/app/rigid_deform.cc:
 13-41 and src/app/cad_deform.cc:22-61 (with fewer than four arguments the
@@ -20,6 +21,12 @@ the Ceres edge residual being lambda*(p1 - p2 - v)), ``--steps`` Adam steps at
   GraphLossFunction objective (rigidity = lambda, DF gradient mask d < 0.03).
   With flow_output, snapshots every ``--flow-every`` steps are written in the
   reference's flow format (cad_deform.cc:90-114).
+* inverse_deform: the reference's Python script (src/python/inverse_deform.py):
+  RigidLossLayer (64^3 grid) plus ReverseLossLayer, loss = 10*rigid +
+  reverse, torch Adam (lr 1e-3) for up to ``--steps`` (10000) iterations,
+  stopping when the loss printed every 100 iterations rises, then Finalize.
+  The layers run on the GPU kernels (the reverse loss's nearest-point query
+  included) and so does Adam.
 """
 import argparse
 import sys
@@ -27,11 +34,12 @@ import sys
 import numpy as np
 import torch
 
-from . import fused, meshops, objio
+from . import fused, layers, meshops, objio
 from . import pyDeform as PD
 
 RIGID_USAGE = ("./rigid_deform source.obj reference.obj output.obj [GRID_RESOLUTION=64] "
                "[MESH_RESOLUTION=5000] [lambda=1] [symmetry=0]")
+INVERSE_USAGE = "inverse_deform.py source.obj reference.obj output.obj"
 CAD_USAGE = ("./cad_deform cad.obj reference.obj output.obj [GRID_RESOLUTION=64] [MESH_RESOLUTION=5000] "
              "[lambda=1] [symmetry=0] [flow_output=filename]")
 
@@ -146,18 +154,68 @@ def cad_deform(argv, steps=1000, lr=1e-3, flow_every=50):
     return 0
 
 
+def inverse_fit(src_V, src_F, tar_V, tar_F, steps=10000, lr=1e-3, log=print):
+    """inverse_deform.py:17-45 on the GPU; returns the fitted source vertices
+    in the source's coordinates and the iterations run."""
+    dev = torch.device("cuda", torch.cuda.current_device())
+    sV = torch.from_numpy(np.ascontiguousarray(src_V, np.float32)).to(dev)
+    sF = torch.from_numpy(np.ascontiguousarray(src_F, np.int32)).to(dev)
+    tV = torch.from_numpy(np.ascontiguousarray(tar_V, np.float32)).to(dev)
+    tF = torch.from_numpy(np.ascontiguousarray(tar_F, np.int32)).to(dev)
+    rigid = layers.RigidLossLayer(sV, sF, tV, tF)
+    reverse = layers.ReverseLossLayer()
+    pid = int(rigid.param_id)
+    P = torch.nn.Parameter(sV)
+    opt = torch.optim.Adam([P], lr=lr)
+    PD.NormalizeByTemplate(tV, pid)
+    prev = 1e30
+    it = 0
+    for it in range(steps):
+        opt.zero_grad()
+        loss_src2tar = rigid(P, sF)
+        loss_tar2src = reverse(P, tV)
+        loss = loss_src2tar * 10 + loss_tar2src
+        loss.backward()
+        opt.step()
+        if it % 100 == 0:
+            lv = loss.item()
+            log("iter=%d loss=%.6f loss_tar2src=%.6f" % (it, lv, np.sqrt(loss_tar2src.item() / tV.shape[0])))
+            if lv > prev:
+                break
+            prev = lv
+    out = P.detach().clone()
+    layers.Finalize(out, pid)
+    PD.ReleaseTemplate(pid)
+    return out.cpu().numpy().astype(np.float64), it + 1
+
+
+def inverse_deform(argv, steps=10000, lr=1e-3):
+    if len(argv) < 3:
+        print(INVERSE_USAGE)
+        return 0
+    src, ref, out = argv[:3]
+    sV, sF = _load(src)
+    rV, rF = _load(ref)
+    V, _ = inverse_fit(sV, sF, rV, rF, steps=steps, lr=lr)
+    objio.write_obj(out, V, sF)
+    return 0
+
+
 def main(argv=None):
     argv = list(sys.argv[1:] if argv is None else argv)
     ap = argparse.ArgumentParser(prog="python -m meshode_gb300.cli", add_help=True)
-    ap.add_argument("program", choices=["rigid_deform", "cad_deform"])
-    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("program", choices=["rigid_deform", "cad_deform", "inverse_deform"])
+    ap.add_argument("--steps", type=int, default=None,
+                    help="Adam steps (rigid/cad: 1000; inverse: at most 10000)")
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--flow-every", type=int, default=50)
     ap.add_argument("args", nargs="*")
     a = ap.parse_intermixed_args(argv)
     if a.program == "rigid_deform":
-        return rigid_deform(a.args, steps=a.steps, lr=a.lr)
-    return cad_deform(a.args, steps=a.steps, lr=a.lr, flow_every=a.flow_every)
+        return rigid_deform(a.args, steps=a.steps or 1000, lr=a.lr)
+    if a.program == "inverse_deform":
+        return inverse_deform(a.args, steps=a.steps or 10000, lr=a.lr)
+    return cad_deform(a.args, steps=a.steps or 1000, lr=a.lr, flow_every=a.flow_every)
 
 
 if __name__ == "__main__":

@@ -448,3 +448,20 @@ def reverse_loss(src_V, tar_V):
     loss = src_c - tar_V
     loss = 0.5 * (loss * loss).sum()
     return loss, ii
+
+
+def inverse_fit(src_V, src_F, tar_V, pid, steps, lr=1e-3):
+    """The loop of src/python/inverse_deform.py:26-38 on the CPU (without its
+    early stop): RigidLossFunction (oracle gradient) * 10 + ReverseLossLayer
+    (cKDTree + torch autograd), torch.optim.Adam.  src_V and tar_V are
+    normalised by the template already.  Returns the fitted vertices."""
+    V = torch.nn.Parameter(src_V.clone())
+    opt = torch.optim.Adam([V], lr=lr)
+    for _ in range(steps):
+        opt.zero_grad()
+        loss_r, _ = reverse_loss(V, tar_V)
+        loss_r.backward()
+        with torch.no_grad():
+            V.grad += rigid_grad(V.data, src_F, pid) * 10
+        opt.step()
+    return V.detach()

@@ -99,6 +99,8 @@ def test_cli_usage_without_gpu(capsys):
     assert "GRID_RESOLUTION" in capsys.readouterr().out
     assert cli.main(["cad_deform"]) == 0
     assert "flow_output" in capsys.readouterr().out
+    assert cli.main(["inverse_deform", "a.obj"]) == 0
+    assert "inverse_deform.py source.obj" in capsys.readouterr().out
 
 
 def test_autotune_buckets():
