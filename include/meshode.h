@@ -416,6 +416,25 @@ int mo_reverse_loss_backward(const float* src, int64_t ns, const float* tar, int
                              int32_t* status_out, void* stream);
 
 /* ------------------------------------------------------------------------
+ * Sparse linear propagation.  Replaces SolveLinear (src/interface/
+ * linear_layer.cc:5-79): LinearEstimation (src/lib/linear.cc:10-112; with_rot
+ * 0) and LinearEstimationWithRot (linear.cc:114-230; with_rot 1), in place
+ * on V (float [nv,3], read and written like the reference's tensor).  The
+ * reference factorises the assembled system with SimplicialLDLT; here it is
+ * solved matrix-free by Jacobi-preconditioned conjugate gradients in double,
+ * from x0 = V, until every coordinate's relative residual is <= tol (or
+ * max_iter iterations: MO_ERR_DEVICE).  with_rot 0: F [nf,3] and E [ne,2]
+ * give the edge springs, ref [nv] the graph node of every vertex, G [ng,3]
+ * the graph positions.  with_rot 1: F only (E, ref ignored), G [nv,3] the
+ * per-vertex targets (ng == nv).  Synchronises `stream`.
+ * ------------------------------------------------------------------------ */
+size_t mo_solve_linear_scratch_bytes(int64_t nv, int64_t nf, int64_t ne, int64_t ng, int with_rot);
+int mo_solve_linear(float* V, int64_t nv, const int32_t* F, int64_t nf, const int32_t* E, int64_t ne,
+                    const int32_t* ref, const float* G, int64_t ng, double rigidity, int with_rot, double tol,
+                    int max_iter, void* scratch, size_t scratch_bytes, int* iters_out, double* rel_residual_out,
+                    void* stream);
+
+/* ------------------------------------------------------------------------
  * Velocity-field ODE deformation (the NeuralODE variant,
  * src/python/layers/neuralode_fast.py:7-64; here 3 -> m -> m -> m -> 3 with
  * softplus and fixed-step RK4).  The m x m layers are plain GEMMs done by

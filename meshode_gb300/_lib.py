@@ -115,6 +115,9 @@ _SIGS = {
     "mo_reverse_loss_scratch_bytes": (_SZ, [_I64, _I64]),
     "mo_reverse_loss_forward": (_I, [_P, _I64, _P, _I64, _P, _P, _P, _SZ, _P, _P]),
     "mo_reverse_loss_backward": (_I, [_P, _I64, _P, _I64, _P, _P, _P, _P, _SZ, _P, _P]),
+    "mo_solve_linear_scratch_bytes": (_SZ, [_I64, _I64, _I64, _I64, _I]),
+    "mo_solve_linear": (_I, [_P, _I64, _P, _I64, _P, _I64, _P, _P, _I64, ctypes.c_double, _I, ctypes.c_double, _I,
+                             _P, _SZ, _P, _P, _P]),
     "mo_pool_create": (_I, [_P, _P]),
     "mo_pool_destroy": (_I, [_P]),
     "mo_pool_submit": (_I, [_P, _P, _P]),

@@ -96,6 +96,16 @@ class GraphLossLayer(nn.Module):
         return GraphLossFunction.apply(src_V, src_E, self.rigidity2, int(self.param_id))
 
 
+def GraphFinalize(src_V, src_F, src_E, src_to_graph, graph_V, rigidity, param_id):
+    """graph_loss_layer.py:62-66 (the module's second Finalize): propagate the
+    fitted graph back to the full mesh with SolveLinear (LinearEstimation) in
+    the template's normalised frame, in place on src_V."""
+    pid = int(param_id)
+    pyDeform.NormalizeByTemplate(src_V, pid)
+    pyDeform.SolveLinear(src_V, src_F, src_E, src_to_graph, graph_V, rigidity, 0)
+    pyDeform.DenormalizeByTemplate(src_V, pid)
+
+
 class ReverseLossFunction(Function):
     """reverse_loss_layer.py:14-25: ii = nearest source vertex of every
     target vertex (cKDTree in the reference, an LBVH query here), loss =

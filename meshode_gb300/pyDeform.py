@@ -141,8 +141,47 @@ def LoadCadMesh(filename):
     raise NotImplementedError("LoadCadMesh (CGAL remeshing) is outside the GPU deformation hot path")
 
 
-def SolveLinear(*args, **kwargs):
-    raise NotImplementedError("SolveLinear (sparse linear propagation) is outside the GPU deformation hot path")
+def SolveLinear(tensorV, tensorF, tensorE, tensorRef, tensorGraphV, rigidity, with_rot=0, tol=1e-13,
+                max_iter=200000):
+    """In place on tensorV (linear_layer.cc:5-79): with_rot 0, LinearEstimation
+    (linear.cc:10-112) -- each vertex pulled to its graph node's position
+    (tensorRef [n] int32 into tensorGraphV [g,3]) through the cell means,
+    rigidity springs on the faces' half-edges and on tensorE; with_rot 1,
+    LinearEstimationWithRot (linear.cc:114-230) -- tensorGraphV [n,3] the
+    per-vertex targets, springs carrying each vertex's rotation and scale.
+    Solved in double by preconditioned conjugate gradients on the GPU
+    (relative residual <= tol); returns (iterations, relative residual)."""
+    _check_vertices(tensorV)
+    _check_indices(tensorF, 3, "F")
+    _check_vertices(tensorGraphV, "GraphV")
+    dev = _cuda_device()
+    nv = int(tensorV.shape[0])
+    with_rot = 1 if with_rot else 0
+    F = _on_device(tensorF, dev)
+    G = _on_device(tensorGraphV, dev)
+    if with_rot:
+        if int(G.shape[0]) != nv:
+            raise RuntimeError("SolveLinear with_rot needs one target per vertex")
+        E = ref = None
+        ne = 0
+    else:
+        _check_indices(tensorE, 2, "E")
+        if not isinstance(tensorRef, torch.Tensor) or tensorRef.dtype != torch.int32 or tensorRef.dim() != 1 \
+                or int(tensorRef.shape[0]) != nv:
+            raise RuntimeError("references must be an int32 tensor [n]")
+        E = _on_device(tensorE, dev)
+        ref = _on_device(tensorRef, dev)
+        ne = int(E.shape[0])
+    work = tensorV if (tensorV.is_cuda and tensorV.is_contiguous()) else _on_device(tensorV, dev)
+    it = ctypes.c_int()
+    res = ctypes.c_double()
+    call("mo_solve_linear", ptr(work), nv, ptr(F), int(F.shape[0]), ptr(E), ne, ptr(ref), ptr(G),
+         int(G.shape[0]), float(rigidity), with_rot, float(tol), int(max_iter), None, 0, ctypes.byref(it),
+         ctypes.byref(res), stream_ptr())
+    if work is not tensorV:
+        with torch.no_grad():
+            tensorV.copy_(work)
+    return it.value, res.value
 
 
 def StoreCadInformation(*args, **kwargs):

@@ -465,3 +465,73 @@ def inverse_fit(src_V, src_F, tar_V, pid, steps, lr=1e-3):
             V.grad += rigid_grad(V.data, src_F, pid) * 10
         opt.step()
     return V.detach()
+
+
+def solve_linear(V, F, E, ref, G, rigidity, with_rot=0):
+    """SolveLinear (src/interface/linear_layer.cc:5-79) on the CPU: the
+    system of LinearEstimation (src/lib/linear.cc:10-112) or
+    LinearEstimationWithRot (linear.cc:114-230) assembled entry by entry as
+    the reference does (duplicates summed), solved directly in double
+    (scipy.sparse.linalg.spsolve instead of Eigen's SimplicialLDLT: the same
+    solution up to rounding).  Returns the new float32 vertices."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spl
+    V = np.asarray(V, np.float32).astype(np.float64)
+    F = np.asarray(F, np.int64).reshape(-1, 3)
+    G = np.asarray(G, np.float32).astype(np.float64)
+    n = V.shape[0]
+    rows, cols, vals = [], [], []
+    B = np.zeros((n, 3))
+    face_edges = np.stack([F[:, [0, 1, 2]].reshape(-1), F[:, [1, 2, 0]].reshape(-1)], 1)
+    if not with_rot:
+        ref = np.asarray(ref, np.int64)
+        E = np.asarray(E, np.int64).reshape(-1, 2)
+        for g in range(G.shape[0]):
+            cell = np.flatnonzero(ref == g)
+            if cell.size == 0:
+                continue
+            w = 1.0 / cell.size
+            jj, kk = np.meshgrid(cell, cell, indexing="ij")
+            rows.append(jj.reshape(-1)); cols.append(kk.reshape(-1)); vals.append(np.full(jj.size, w * w))
+            B[cell] += w * G[g]
+        rows.append(np.arange(n)); cols.append(np.arange(n)); vals.append(np.full(n, 1e-6))
+        B += 1e-6 * G[ref]
+        edges = np.concatenate([face_edges, E])
+        a, b = edges[:, 0], edges[:, 1]
+        reg = rigidity * 2e-2 / (np.linalg.norm(V[a] - V[b], axis=1) + 1e-8)
+        reg = reg * reg
+        rows += [a, a, b, b]; cols += [a, b, a, b]; vals += [reg, -reg, -reg, reg]
+        np.add.at(B, a, reg[:, None] * (V[a] - V[b]))
+        np.add.at(B, b, reg[:, None] * (V[b] - V[a]))
+    else:
+        links = [set() for _ in range(n)]
+        for a, b in face_edges:
+            links[a].add(b)
+            links[b].add(a)
+        R = np.zeros((n, 3, 3))
+        scale = np.zeros(n)
+        for i in range(n):
+            M = np.zeros((3, 3))
+            lo = lc = 0.0
+            for p in sorted(links[i]):
+                d1 = V[p] - V[i]
+                d2 = G[p] - G[i]
+                lo += np.linalg.norm(d1)
+                lc += np.linalg.norm(d2)
+                M += np.outer(d2, d1)
+            scale[i] = lc / (lo + 1e-8)
+            U, _, Vt = np.linalg.svd(M)
+            R[i] = U @ Vt
+        rows.append(np.arange(n)); cols.append(np.arange(n)); vals.append(np.ones(n))
+        B += G
+        for j in (0, 1):
+            a, b = face_edges[:, j], face_edges[:, 1 - j]
+            off = V[b] - V[a]
+            reg = 1.0 * 2e-2 / np.linalg.norm(off, axis=1) * rigidity
+            off = scale[a, None] * np.einsum("nij,nj->ni", R[a], off)
+            rows += [a, a, b, b]; cols += [a, b, a, b]; vals += [reg, -reg, -reg, reg]
+            np.add.at(B, a, -reg[:, None] * off)
+            np.add.at(B, b, reg[:, None] * off)
+    A = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(n, n))
+    X = spl.spsolve(A.tocsc(), B)
+    return X.astype(np.float32)

@@ -235,3 +235,25 @@ def test_reverse_loss_known_answer(orc):
     assert float(loss) == pytest.approx(0.5 * (0.125 ** 2 + 0.25 ** 2 + 0.25 ** 2 + 0.5 ** 2))
     loss.backward()
     assert torch.equal(src.grad, torch.tensor([[-0.25, 0.0, 0.0], [0.125 + 0.25, -0.5, 0.0]]))
+
+
+def test_solve_linear_known_answer(orc):
+    """Two vertices, one face-less edge, each its own graph node: the system
+    ((w^2 + 1e-6) I + reg L) x = (w + 1e-6) G + reg L V has the closed form
+    below (w = 1)."""
+    V = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0]], np.float32)
+    G = np.array([[0.0, 0.5, 0.0], [2.0, 0.5, 0.0]], np.float32)
+    F = np.zeros((0, 3), np.int32)
+    E = np.array([[0, 1]], np.int32)
+    ref = np.array([0, 1], np.int32)
+    X = orc.solve_linear(V, F, E, ref, G, 1.0, with_rot=0).astype(np.float64)
+    reg = (0.02 / (1.0 + 1e-8)) ** 2
+    a = 1.0 + 1e-6
+    # symmetric system per coordinate: [[a+reg, -reg], [-reg, a+reg]] x = b
+    for c in range(3):
+        b0 = a * G[0, c] + reg * (V[0, c] - V[1, c])
+        b1 = a * G[1, c] + reg * (V[1, c] - V[0, c])
+        det = (a + reg) ** 2 - reg ** 2
+        x0 = ((a + reg) * b0 + reg * b1) / det
+        x1 = (reg * b0 + (a + reg) * b1) / det
+        assert X[0, c] == pytest.approx(x0, abs=1e-7) and X[1, c] == pytest.approx(x1, abs=1e-7)
