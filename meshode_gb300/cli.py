@@ -5,6 +5,7 @@
     python -m meshode_gb300.cli cad_deform cad.obj reference.obj output.obj \\
         [GRID_RESOLUTION=64] [MESH_RESOLUTION=5000] [lambda=1] [symmetry=0] [flow_output]
     python -m meshode_gb300.cli inverse_deform source.obj reference.obj output.obj
+    python -m meshode_gb300.cli cad_deform2 --source cad.obj --target cad-ref.obj --output out.obj [--rigidity 1]
 
 Positional arguments, defaults and their order follow src/app/rigid_deform.cc:
 13-41 and src/app/cad_deform.cc:22-61 (with fewer than four arguments the
@@ -14,13 +15,19 @@ Levenberg-Marquardt: same objective (0.5*sum d^2 + lambda^2 * 0.5*sum r^2,
 the Ceres edge residual being lambda*(p1 - p2 - v)), ``--steps`` Adam steps at
 ``--lr``.  Differences, by necessity:
 * rigid_deform: as the reference, MESH_RESOLUTION is parsed and unused.
-* cad_deform: the reference remeshes the CAD model with CGAL and optimises a
-  representative graph (subdivision.cc); here the model is cleaned like the
-  reference (RemoveDegenerated, MergeDuplex), midpoint-subdivided to at least
-  MESH_RESOLUTION vertices, and its mesh edges are the graph, fitted with the
-  GraphLossFunction objective (rigidity = lambda, DF gradient mask d < 0.03).
-  With flow_output, snapshots every ``--flow-every`` steps are written in the
-  reference's flow format (cad_deform.cc:90-114).
+* cad_deform: as the reference, the CAD model is cleaned (RemoveDegenerated,
+  MergeDuplex), remeshed at 0.02 with its geometry neighbours and its
+  representative graph (Subdivision, restated in cadmesh with SciPy's
+  Delaunay); the graph is fitted (DeformGraph's objective: 0.5*sum d^2 +
+  lambda^2 * 0.5*sum r^2 over the graph edges) and SolveLinear (rigidity 2,
+  Subdivision::LinearSolve) carries the fit to every remeshed vertex.  With
+  flow_output every remeshed vertex is fitted instead (DeformSubdivision,
+  with the neighbour pairs as uniformly weighted edges where the reference
+  uses its length-adaptive edge loss) and snapshots every ``--flow-every``
+  steps are written in the reference's flow format (cad_deform.cc:90-114).
+  MESH_RESOLUTION is parsed and unused, as in the reference.
+* cad_deform2: the Python script src/python/cad_deform2.py (its own
+  --source/--target/--output/--rigidity options).
 * inverse_deform: the reference's Python script (src/python/inverse_deform.py):
   RigidLossLayer (64^3 grid) plus ReverseLossLayer, loss = 10*rigid +
   reverse, torch Adam (lr 1e-3) for up to ``--steps`` (10000) iterations,
@@ -34,7 +41,7 @@ import sys
 import numpy as np
 import torch
 
-from . import fused, layers, meshops, objio
+from . import cadmesh, fused, layers, meshops, objio
 from . import pyDeform as PD
 
 RIGID_USAGE = ("./rigid_deform source.obj reference.obj output.obj [GRID_RESOLUTION=64] "
@@ -54,23 +61,28 @@ def _load(path):
     return V, F
 
 
-def _fit(src_V, src_F, tar_V, tar_F, N, lam, steps, lr, graph=False, flow_every=0, log=print):
+def _fit(src_V, src_F, tar_V, tar_F, N, lam, steps, lr, edges=None, mask=False, flow_every=0, log=print,
+         keep=False):
+    """The fused GPU Adam loop: source normalised by the target's template,
+    edges = the faces' half-edges (StoreRigidityInformation) or an explicit
+    list (StoreGraphInformation), edge weight lam^2, the d < 0.03 DF mask
+    when `mask`.  Returns the fitted vertices denormalised (float64 numpy)
+    and the flow snapshots; with keep=True, the normalised device tensor, the
+    snapshots and the template id instead (the caller releases it)."""
     dev = torch.device("cuda", torch.cuda.current_device())
     tV = torch.from_numpy(np.ascontiguousarray(tar_V, np.float32)).to(dev)
     tF = torch.from_numpy(np.ascontiguousarray(tar_F, np.int32)).to(dev)
     pid = PD.InitializeDeformTemplate(tV, tF, 0, N)
     V = torch.from_numpy(np.ascontiguousarray(src_V, np.float32)).to(dev)
     PD.NormalizeByTemplate(V, pid)
-    F = torch.from_numpy(np.ascontiguousarray(src_F, np.int32)).to(dev)
     w = float(np.float32(lam * lam))
-    if graph:
-        from . import meshgen
-        E = torch.from_numpy(meshgen.edges_from_faces(np.asarray(src_F))).to(dev)
+    if edges is not None:
+        E = torch.from_numpy(np.ascontiguousarray(edges, np.int32)).to(dev)
         PD.StoreGraphInformation(V, E, pid)
-        mask = float(np.float32(0.5 * 0.03 * 0.03))
     else:
+        F = torch.from_numpy(np.ascontiguousarray(src_F, np.int32)).to(dev)
         PD.StoreRigidityInformation(V, F, pid)
-        mask = None
+    mask = float(np.float32(0.5 * 0.03 * 0.03)) if mask else None
     pr = fused.pair_from_template(pid, V, steps, lr=lr, w_edge=w, mask_thresh=mask)
     group = 25 if not flow_every else max(1, min(25, flow_every))
     runner = fused.StepGroupRunner(dev, 1, pr.ntiles, group_steps=group)
@@ -89,6 +101,8 @@ def _fit(src_V, src_F, tar_V, tar_F, N, lam, steps, lr, graph=False, flow_every=
             PD.DenormalizeByTemplate(snap, pid)
             flow.append(snap.cpu().numpy().astype(np.float64))
     out = pr.positions()
+    if keep:
+        return out, flow, pid
     PD.DenormalizeByTemplate(out, pid)
     PD.ReleaseTemplate(pid)
     return out.cpu().numpy().astype(np.float64), flow
@@ -143,14 +157,80 @@ def cad_deform(argv, steps=1000, lr=1e-3, flow_every=50):
         rV, rF = meshops.reflection_symmetrize(rV, rF)
     cV, cF = meshops.remove_degenerated(cV, cF)
     cV, cF = meshops.merge_duplex(cV, cF)
-    cV, cF = meshops.subdivide_to(cV, cF, mres)
     print("Source:\t\tNum vertices: %d\tNum faces: %d" % (cV.shape[0], cF.shape[0]))
     print("Reference:\tNum vertices: %d\tNum faces: %d\n" % (rV.shape[0], rF.shape[0]))
-    V, flow = _fit(cV, cF, rV, rF, N, lam, steps, lr, graph=True, flow_every=flow_every if flow_file else 0)
-    if flow_file:
-        _write_flow(flow_file, cV, flow)
+    # Subdivision (cad_deform.cc:46-49): remesh at 0.02, neighbours, graph
+    Vs = Fs = E = ref_ = GV = GE = None
+    Vs, Fs = cadmesh.subdivide(cV, cF, cadmesh.SUBDIV_LEN)
+    E = cadmesh.geometry_neighbors(Vs, Fs, cadmesh.NEIGHBOR_STEP)
+    if not flow_file:
+        # Deformer::DeformGraph: the representative graph fitted (distance +
+        # lambda * edge residuals), then Subdivision::LinearSolve propagates
+        # it to every remeshed vertex (LinearEstimation, rigidity 2)
+        ref_, GV, GE = cadmesh.representative_graph(Vs, Fs, E, cadmesh.GRAPH_STEP)
+        G, _, pid = _fit(GV, None, rV, rF, N, lam, steps, lr, edges=GE, keep=True)
+        dev = G.device
+        V = torch.from_numpy(Vs.astype(np.float32)).to(dev)
+        PD.NormalizeByTemplate(V, pid)
+        PD.SolveLinear(V, torch.from_numpy(Fs.astype(np.int32)), torch.from_numpy(E.astype(np.int32)),
+                       torch.from_numpy(ref_.astype(np.int32)), G, 2.0, 0)
+        PD.DenormalizeByTemplate(V, pid)
+        PD.ReleaseTemplate(pid)
+        Vout = V.cpu().numpy().astype(np.float64)
+    else:
+        # Deformer::DeformSubdivision: every remeshed vertex fitted, edges the
+        # neighbour pairs (which include the mesh edges), flow snapshots
+        Vout, flow = _fit(Vs, Fs, rV, rF, N, lam, steps, lr, edges=E, flow_every=flow_every)
+        _write_flow(flow_file, Vs, flow)
     print("Deformed")
-    objio.write_obj(out, V, cF)
+    objio.write_obj(out, Vout, Fs)
+    return 0
+
+
+def cad_deform2(argv, steps=10000, lr=1e-3, log=print):
+    """src/python/cad_deform2.py: both models through LoadCadMesh; the
+    source's representative graph fitted with GraphLossLayer + the reverse
+    loss against the target's graph (each divided by its vertex count), torch
+    Adam, stopping when neither loss improves by 1e-6 between the reports
+    every 100 iterations; then the graph Finalize (SolveLinear, rigidity 1)
+    and SaveMesh of the remeshed source."""
+    ap = argparse.ArgumentParser(prog="cad_deform2")
+    ap.add_argument("--source", default="../data/cad-source.obj")
+    ap.add_argument("--target", default="../data/cad-target.obj")
+    ap.add_argument("--output", default="./cad-output.obj")
+    ap.add_argument("--rigidity", default="1")
+    a = ap.parse_args(argv)
+    rigidity = float(a.rigidity)
+    src_V, src_F, src_E, src_to_graph, graph_V, graph_E = PD.LoadCadMesh(a.source)
+    tar_V, tar_F, _, _, graph_V_tar, _ = PD.LoadCadMesh(a.target)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    graph_V = graph_V.to(dev)
+    graph_E = graph_E.to(dev)
+    graph_deform = layers.GraphLossLayer(graph_V, graph_E, tar_V, tar_F, rigidity)
+    param_id = graph_deform.param_id
+    reverse_deform = layers.ReverseLossLayer()
+    graph_V = torch.nn.Parameter(graph_V)
+    optimizer = torch.optim.Adam([graph_V], lr=lr)
+    graph_V_tar = graph_V_tar.to(dev)
+    PD.NormalizeByTemplate(graph_V_tar, int(param_id))
+    prev_src, prev_tar = 1e30, 1e30
+    for it in range(steps):
+        optimizer.zero_grad()
+        loss_src2tar = graph_deform(graph_V, graph_E)
+        loss_tar2src = reverse_deform(graph_V, graph_V_tar)
+        loss = loss_src2tar / graph_V.shape[0] + loss_tar2src / graph_V_tar.shape[0]
+        loss.backward()
+        optimizer.step()
+        if it % 100 == 0:
+            cur_src = float(np.sqrt(loss_src2tar.item() / graph_V.shape[0]))
+            cur_tar = float(np.sqrt(loss_tar2src.item() / graph_V_tar.shape[0]))
+            log("iter=%d, loss_src2tar=%.6f loss_tar2src=%.6f" % (it, cur_src, cur_tar))
+            if prev_src - cur_src < 1e-6 and prev_tar - cur_tar < 1e-6:
+                break
+            prev_src, prev_tar = cur_src, cur_tar
+    layers.GraphFinalize(src_V, src_F, src_E, src_to_graph, graph_V.detach(), 1, param_id)
+    PD.SaveMesh(a.output, src_V, src_F)
+    PD.ReleaseTemplate(int(param_id))
     return 0
 
 
@@ -204,12 +284,20 @@ def inverse_deform(argv, steps=10000, lr=1e-3):
 def main(argv=None):
     argv = list(sys.argv[1:] if argv is None else argv)
     ap = argparse.ArgumentParser(prog="python -m meshode_gb300.cli", add_help=True)
-    ap.add_argument("program", choices=["rigid_deform", "cad_deform", "inverse_deform"])
+    ap.add_argument("program", choices=["rigid_deform", "cad_deform", "inverse_deform", "cad_deform2"])
     ap.add_argument("--steps", type=int, default=None,
                     help="Adam steps (rigid/cad: 1000; inverse: at most 10000)")
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--flow-every", type=int, default=50)
     ap.add_argument("args", nargs="*")
+    if argv and argv[0] == "cad_deform2":  # the script's own --source/--target/--output/--rigidity
+        rest = argv[1:]
+        steps = 10000
+        if "--steps" in rest:
+            k = rest.index("--steps")
+            steps = int(rest[k + 1])
+            rest = rest[:k] + rest[k + 2:]
+        return cad_deform2(rest, steps=steps)
     a = ap.parse_intermixed_args(argv)
     if a.program == "rigid_deform":
         return rigid_deform(a.args, steps=a.steps or 1000, lr=a.lr)

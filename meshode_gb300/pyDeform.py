@@ -138,7 +138,12 @@ def SaveMesh(filename, tensorV, tensorF):
 
 
 def LoadCadMesh(filename):
-    raise NotImplementedError("LoadCadMesh (CGAL remeshing) is outside the GPU deformation hot path")
+    """mesh_tensor.cc:102-178: [V f32 [n,3], F i32 [m,3], E i32 [k,2]
+    (geometry neighbour pairs), src_to_graph i32 [n,1], graph V f32 [g,3],
+    graph E i32 [q,2]] as CPU tensors -- the CAD model remeshed at 0.02 with
+    its representative graph (restated with SciPy's Delaunay; see cadmesh)."""
+    from . import cadmesh
+    return [torch.from_numpy(np.ascontiguousarray(a)) for a in cadmesh.load_cad_mesh(filename)]
 
 
 def SolveLinear(tensorV, tensorF, tensorE, tensorRef, tensorGraphV, rigidity, with_rot=0, tol=1e-13,
@@ -166,11 +171,12 @@ def SolveLinear(tensorV, tensorF, tensorE, tensorRef, tensorGraphV, rigidity, wi
         ne = 0
     else:
         _check_indices(tensorE, 2, "E")
-        if not isinstance(tensorRef, torch.Tensor) or tensorRef.dtype != torch.int32 or tensorRef.dim() != 1 \
-                or int(tensorRef.shape[0]) != nv:
-            raise RuntimeError("references must be an int32 tensor [n]")
+        # LoadCadMesh returns the references as [n,1]; [n] is accepted too
+        if not isinstance(tensorRef, torch.Tensor) or tensorRef.dtype != torch.int32 or tensorRef.numel() != nv \
+                or not (tensorRef.dim() == 1 or (tensorRef.dim() == 2 and tensorRef.shape[1] == 1)):
+            raise RuntimeError("references must be an int32 tensor [n] or [n,1]")
         E = _on_device(tensorE, dev)
-        ref = _on_device(tensorRef, dev)
+        ref = _on_device(tensorRef.reshape(-1), dev)
         ne = int(E.shape[0])
     work = tensorV if (tensorV.is_cuda and tensorV.is_contiguous()) else _on_device(tensorV, dev)
     it = ctypes.c_int()

@@ -39,8 +39,10 @@ def test_validation_errors_without_gpu():
         PD.InitializeDeformTemplate(torch.zeros(5, 3), torch.zeros(0, 3, dtype=torch.int32), 0, 64)
     with pytest.raises(RuntimeError):
         PD.InitializeDeformTemplate(torch.zeros(5, 3), torch.zeros(2, 3, dtype=torch.int32), 0, 1)
-    with pytest.raises(NotImplementedError):
+    with pytest.raises(FileNotFoundError):
         PD.LoadCadMesh("x.obj")
+    with pytest.raises(NotImplementedError):
+        PD.StoreCadInformation(None, None, None, 0)
 
 
 def test_generators():
