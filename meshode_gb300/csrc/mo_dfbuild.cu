@@ -273,7 +273,7 @@ __device__ __forceinline__ int kdelta(const uint32_t* __restrict__ k, int n, int
 }
 
 __global__ void k_karras(const uint32_t* __restrict__ k, int n, float4* __restrict__ nodes,
-                         int* __restrict__ parent, int* __restrict__ flags) {
+                         int* __restrict__ parent, int* __restrict__ flags, int2* __restrict__ range) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
     const int d = (kdelta(k, n, i, i + 1) - kdelta(k, n, i, i - 1)) >= 0 ? 1 : -1;
@@ -292,6 +292,7 @@ __global__ void k_karras(const uint32_t* __restrict__ k, int n, float4* __restri
     } while (t > 1);
     const int gamma = i + s * d + (d < 0 ? -1 : 0);
     const int lo = min(i, j), hi = max(i, j);
+    if (range) range[i] = make_int2(lo, hi);
     const int left = (lo == gamma) ? ~gamma : gamma;
     const int right = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
     nodes[4 * (int64_t)i].w = __int_as_float(left);
@@ -342,6 +343,34 @@ __global__ void k_refit(const float4* __restrict__ boxes, int n, float4* nodes, 
     for (int c = 0; c < 3; ++c) {
         rootbox[c] = lo[c];
         rootbox[3 + c] = hi[c];
+    }
+}
+
+// Leaf buckets: a child whose subtree holds at most `k` triangles becomes a
+// leaf bucket -- id ~first leaf, count in the .w lane of node word 2 (left)
+// or 3 (right); a single-triangle leaf has count 1, an internal child 0.
+// The traversal then tests the bucket's (contiguous, sorted) triangles
+// directly instead of descending the bottom levels of the tree.
+constexpr int DF_BUCKET = 6;
+
+__global__ void k_buckets(float4* __restrict__ nodes, const int2* __restrict__ range, int n, int k) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    float4* nd = nodes + 4 * (int64_t)i;
+    for (int side = 0; side < 2; ++side) {
+        const int c = __float_as_int(nd[side].w);
+        int id = c, cnt = 0;
+        if (c < 0) {
+            cnt = 1;
+        } else {
+            const int2 r = range[c];
+            if (r.y - r.x + 1 <= k) {
+                id = ~r.x;
+                cnt = r.y - r.x + 1;
+            }
+        }
+        nd[side].w = __int_as_float(id);
+        nd[2 + side].w = __int_as_float(cnt);
     }
 }
 
@@ -415,19 +444,20 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) k_df_lbvh(const float4* __res
             const float4* nd = nodes + 4 * (int64_t)node;
             const float4 a = __ldg(nd), b = __ldg(nd + 1), c = __ldg(nd + 2), d = __ldg(nd + 3);
             const int L = __float_as_int(a.w), R = __float_as_int(b.w);
+            const int cl = __float_as_int(c.w), cr = __float_as_int(d.w);  // bucket sizes (0: internal)
             const float dl = box_d2(px, py, pz, a, b), dr = box_d2(px, py, pz, c, d);
             bool wl = __any_sync(FULL, dl < lim);
             bool wr = __any_sync(FULL, dr < lim);
-            if (wl && L < 0) {
-                const float t = tri_d2(px, py, pz, load_tri(tris, ~L), best);
+            // the opened buckets' triangles, left then right, one test body
+            const int nl = wl ? cl : 0, nr = wr ? cr : 0;
+#pragma unroll 1
+            for (int k = 0; k < nl + nr; ++k) {
+                const int tri = k < nl ? ~L + k : ~R + (k - nl);
+                const float t = tri_d2(px, py, pz, load_tri(tris, tri), best);
                 if (valid && t < best) { best = t; lim = slack_bound(best); }
-                wl = false;
             }
-            if (wr && R < 0) {
-                const float t = tri_d2(px, py, pz, load_tri(tris, ~R), best);
-                if (valid && t < best) { best = t; lim = slack_bound(best); }
-                wr = false;
-            }
+            if (cl > 0) wl = false;
+            if (cr > 0) wr = false;
             if (wl && wr) {
                 const unsigned nearer_l = __ballot_sync(FULL, valid && dl <= dr);
                 const unsigned act = __ballot_sync(FULL, valid);
@@ -520,6 +550,7 @@ struct BuildScratch {
     int* hist;
     float* rootbox;
     int* status;
+    int2* range;  // leaves [first, last] of every internal node
     size_t bytes;
 };
 
@@ -547,12 +578,14 @@ static BuildScratch plan_scratch(char* base, int64_t nv, int64_t nf, int method)
         s.parent = reinterpret_cast<int*>(take(sizeof(int) * (size_t)(2 * nf)));
         s.flags = reinterpret_cast<int*>(take(sizeof(int) * (size_t)nf));
         s.hist = reinterpret_cast<int*>(take(sizeof(int) * radix_hist_ints((int)nf)));
+        s.range = reinterpret_cast<int2*>(take(sizeof(int2) * (size_t)(nf > 1 ? nf - 1 : 1)));
     } else {
         s.codes_a = s.codes_b = nullptr;
         s.ids_a = s.ids_b = nullptr;
         s.nodes = nullptr;
         s.boxes = nullptr;
         s.parent = s.flags = s.hist = nullptr;
+        s.range = nullptr;
     }
     s.bytes = o;
     return s;
@@ -660,8 +693,10 @@ extern "C" int mo_df_build_ex(const float* V, int64_t nv, const int32_t* F, int6
             if (e != cudaSuccess) { fail(e, "radix_sort_pairs"); break; }
             k_tri_records<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.ids_a, S.tris, S.boxes); ::mo::note_launch();
             if (nf > 1) {
-                k_karras<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.codes_a, (int)nf, S.nodes, S.parent, S.flags); ::mo::note_launch();
+                k_karras<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.codes_a, (int)nf, S.nodes, S.parent, S.flags, S.range);
+                ::mo::note_launch();
                 k_refit<<<ceil_div(nf, 256), 256, 0, s>>>(S.boxes, (int)nf, S.nodes, S.parent, S.flags, S.rootbox, st); ::mo::note_launch();
+                k_buckets<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.nodes, S.range, (int)nf, DF_BUCKET); ::mo::note_launch();
             }
             launch_df_lbvh(packet, S.nodes, S.tris, (int)nf, N, band, band2, grid_out, st, s);
         }
@@ -719,7 +754,8 @@ extern "C" int mo_lbvh_build(const float* V, int64_t nv, const int32_t* F, int64
     if (e == cudaSuccess) {
         k_tri_records<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.ids_a, S.tris, S.boxes); ::mo::note_launch();
         if (nf > 1) {
-            k_karras<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.codes_a, (int)nf, S.nodes, S.parent, S.flags); ::mo::note_launch();
+            k_karras<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.codes_a, (int)nf, S.nodes, S.parent, S.flags, nullptr);
+            ::mo::note_launch();
             k_refit<<<ceil_div(nf, 256), 256, 0, s>>>(S.boxes, (int)nf, S.nodes, S.parent, S.flags, S.rootbox,
                                                       S.status); ::mo::note_launch();
         }

@@ -36,9 +36,10 @@ __device__ __forceinline__ uint32_t morton30(float x, float y, float z) {
 
 // Children of the n-1 internal nodes from n sorted codes (ties broken by
 // index), parent links (parent[slot] = 2*node + side; leaf k has slot n-1+k)
-// and zeroed refit flags.
+// and zeroed refit flags; range (optional) gets each node's leaves
+// [first, last] (a Karras subtree's leaves are contiguous).
 __global__ void k_karras(const uint32_t* __restrict__ k, int n, float4* __restrict__ nodes,
-                         int* __restrict__ parent, int* __restrict__ flags);
+                         int* __restrict__ parent, int* __restrict__ flags, int2* __restrict__ range);
 // Boxes of every internal node from the n leaf boxes (2 float4 each, lo then
 // hi, in sorted order); the root box goes to rootbox[6].  Bit 2 of status on
 // a malformed parent array.

@@ -429,7 +429,8 @@ extern "C" int mo_nn_query(const float* P, int64_t np, const float* Q, int64_t n
         if (e != cudaSuccess) { rc = cuda_status(e, "radix_sort_pairs"); break; }
         if (np > 1) {
             k_pt_leaves<<<ceil_div(np, 256), 256, 0, s>>>(P, S.ids_a, (int)np, S.boxes); ::mo::note_launch();
-            k_karras<<<ceil_div(np - 1, 256), 256, 0, s>>>(S.codes_a, (int)np, S.nodes, S.parent, S.flags);
+            k_karras<<<ceil_div(np - 1, 256), 256, 0, s>>>(S.codes_a, (int)np, S.nodes, S.parent, S.flags,
+                                                           nullptr);
             ::mo::note_launch();
             k_refit<<<ceil_div(np, 256), 256, 0, s>>>(S.boxes, (int)np, S.nodes, S.parent, S.flags, S.rootbox,
                                                        S.status);
