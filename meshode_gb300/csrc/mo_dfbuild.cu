@@ -346,32 +346,287 @@ __global__ void k_refit(const float4* __restrict__ boxes, int n, float4* nodes, 
     }
 }
 
-// Leaf buckets: a child whose subtree holds at most `k` triangles becomes a
-// leaf bucket -- id ~first leaf, count in the .w lane of node word 2 (left)
-// or 3 (right); a single-triangle leaf has count 1, an internal child 0.
-// The traversal then tests the bucket's (contiguous, sorted) triangles
-// directly instead of descending the bottom levels of the tree.
+// Leaf buckets: a child whose subtree holds at most DF_BUCKET triangles is a
+// bucket -- its record holds ~first leaf and the count (a single triangle:
+// count 1; an internal child: 0) -- and the traversal tests the bucket's
+// contiguous sorted triangles directly instead of descending the bottom
+// levels of the tree.
 constexpr int DF_BUCKET = 6;
 
-__global__ void k_buckets(float4* __restrict__ nodes, const int2* __restrict__ range, int n, int k) {
+// ---------------------------------------------------------------------------
+// Oriented bounding boxes.  Every child of a node is bounded, for the
+// traversal, by a box aligned with its surface patch: axis a3 along the sum
+// of the patch's area-weighted normals, a1 in the patch's plane (a single
+// triangle: along its first edge; otherwise the x or y axis projected on the
+// plane), a2 = a3 x a1, extents measured from an origin corner.  A near-planar
+// patch's box is thin along its normal, so it reaches toward a query point
+// only by the patch's curvature, where an axis-aligned box reaches by the
+// patch's size; far fewer boxes come within a voxel's distance.
+// Subtrees of at most OBB_EXACT triangles get extents from their own
+// vertices; larger ones from the eight corners of their two children's boxes.
+// Every extent is widened by OBB_INFL on both sides, more than the float
+// rounding of the projections at build and query time, so the box contains
+// its triangles' computed points and the distance bound stays below every
+// triangle's computed distance by less than the traversal's slack.
+// ---------------------------------------------------------------------------
+constexpr int OBB_EXACT = 4096;
+constexpr float OBB_INFL = 2e-6f;
+
+struct Obb {
+    float3 o, a1, a2, e;  // origin, axes (a3 = a1 x a2), extents
+};
+
+// a3 exactly as the traversal computes it
+__device__ __forceinline__ float3 obb_a3(float3 a1, float3 a2) {
+    return make_float3(__fsub_rn(__fmul_rn(a1.y, a2.z), __fmul_rn(a1.z, a2.y)),
+                       __fsub_rn(__fmul_rn(a1.z, a2.x), __fmul_rn(a1.x, a2.z)),
+                       __fsub_rn(__fmul_rn(a1.x, a2.y), __fmul_rn(a1.y, a2.x)));
+}
+
+__device__ __forceinline__ float dotf3(float3 a, float x, float y, float z) {
+    return fmaf(a.z, z, fmaf(a.y, y, __fmul_rn(a.x, x)));
+}
+
+__device__ __forceinline__ float3 unit3f(float3 v, float3 fallback) {
+    const float n2 = v.x * v.x + v.y * v.y + v.z * v.z;
+    if (!(n2 > 1e-30f) || !isfinite(n2)) return fallback;
+    const float r = 1.0f / sqrtf(n2);
+    return make_float3(v.x * r, v.y * r, v.z * r);
+}
+
+// Frame from a normal sum and an in-plane hint (NaN hint: project x or y).
+__device__ void obb_frame(float3 nsum, float3 hint, float3& a1, float3& a2) {
+    const float3 a3 = unit3f(nsum, make_float3(0.f, 0.f, 1.f));
+    float3 h = hint;
+    if (!(h.x == h.x)) h = fabsf(a3.x) < 0.9f ? make_float3(1.f, 0.f, 0.f) : make_float3(0.f, 1.f, 0.f);
+    const float d = h.x * a3.x + h.y * a3.y + h.z * a3.z;
+    float3 t = make_float3(h.x - d * a3.x, h.y - d * a3.y, h.z - d * a3.z);
+    const float3 alt = fabsf(a3.x) < 0.9f ? make_float3(1.f - a3.x * a3.x, -a3.x * a3.y, -a3.x * a3.z)
+                                          : make_float3(-a3.y * a3.x, 1.f - a3.y * a3.y, -a3.y * a3.z);
+    a1 = unit3f(t, unit3f(alt, make_float3(1.f, 0.f, 0.f)));
+    a2 = unit3f(make_float3(a3.y * a1.z - a3.z * a1.y, a3.z * a1.x - a3.x * a1.z, a3.x * a1.y - a3.y * a1.x),
+                make_float3(0.f, 1.f, 0.f));
+}
+
+// Running extents of points projected on (a1, a2, a3) relative to r.
+struct Ext {
+    float lo[3], hi[3];
+    __device__ void init() {
+        for (int k = 0; k < 3; ++k) { lo[k] = FLT_MAX; hi[k] = -FLT_MAX; }
+    }
+    __device__ void add(float3 a1, float3 a2, float3 a3, float3 r, float x, float y, float z) {
+        const float qx = __fsub_rn(x, r.x), qy = __fsub_rn(y, r.y), qz = __fsub_rn(z, r.z);
+        const float t[3] = {dotf3(a1, qx, qy, qz), dotf3(a2, qx, qy, qz), dotf3(a3, qx, qy, qz)};
+        for (int k = 0; k < 3; ++k) { lo[k] = fminf(lo[k], t[k]); hi[k] = fmaxf(hi[k], t[k]); }
+    }
+    __device__ Obb finish(float3 a1, float3 a2, float3 a3, float3 r) const {
+        Obb b;
+        b.a1 = a1; b.a2 = a2;
+        float l[3];
+        for (int k = 0; k < 3; ++k) l[k] = lo[k] - OBB_INFL;
+        b.o = make_float3(r.x + l[0] * a1.x + l[1] * a2.x + l[2] * a3.x, r.y + l[0] * a1.y + l[1] * a2.y + l[2] * a3.y,
+                          r.z + l[0] * a1.z + l[1] * a2.z + l[2] * a3.z);
+        b.e = make_float3(hi[0] - lo[0] + 2.f * OBB_INFL, hi[1] - lo[1] + 2.f * OBB_INFL,
+                          hi[2] - lo[2] + 2.f * OBB_INFL);
+        return b;
+    }
+};
+
+// The vertices of sorted triangle k from its record (non-degenerate: a, a +
+// bx ex, a + cx ex + cy ey, within rounding of the input vertices) and its
+// normal scaled by twice its area (zero for a degenerate record).
+__device__ __forceinline__ void rec_tri(const float4* __restrict__ tris, int k, float3 v[3], float3* n,
+                                        float3* edge) {
+    const float4* r = tris + TRI_F4 * (int64_t)k;
+    const float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2), r3 = __ldg(r + 3);
+    v[0] = make_float3(r0.x, r0.y, r0.z);
+    if (r3.w != 0.f) {
+        v[1] = make_float3(fmaf(r0.w, r1.x, r0.x), fmaf(r0.w, r1.y, r0.y), fmaf(r0.w, r1.z, r0.z));
+        v[2] = make_float3(fmaf(r2.w, r2.x, fmaf(r1.w, r1.x, r0.x)), fmaf(r2.w, r2.y, fmaf(r1.w, r1.y, r0.y)),
+                           fmaf(r2.w, r2.z, fmaf(r1.w, r1.z, r0.z)));
+        const float w = r0.w * r2.w;
+        *n = make_float3(r3.x * w, r3.y * w, r3.z * w);
+        *edge = make_float3(r1.x, r1.y, r1.z);
+    } else {
+        v[1] = make_float3(r1.x, r1.y, r1.z);
+        v[2] = make_float3(r2.x, r2.y, r2.z);
+        *n = make_float3(0.f, 0.f, 0.f);
+        *edge = make_float3(r1.x - r0.x, r1.y - r0.y, r1.z - r0.z);
+    }
+}
+
+// The box of one sorted triangle (a1 along its first edge).
+__device__ Obb obb_of_tri(const float4* __restrict__ tris, int k, float3* nsum_out) {
+    float3 v[3], n, edge;
+    rec_tri(tris, k, v, &n, &edge);
+    float3 a1, a2;
+    obb_frame(n, edge, a1, a2);
+    const float3 a3 = obb_a3(a1, a2);
+    Ext x;
+    x.init();
+    for (int c = 0; c < 3; ++c) x.add(a1, a2, a3, v[0], v[c].x, v[c].y, v[c].z);
+    *nsum_out = n;
+    return x.finish(a1, a2, a3, v[0]);
+}
+
+// obb[4*i] = (o, nsum.x) (a1, nsum.y) (a2, nsum.z) (e, -) of internal node i.
+__device__ __forceinline__ void store_obb(float4* __restrict__ obb, int i, const Obb& b, float3 ns) {
+    obb[4 * (int64_t)i] = make_float4(b.o.x, b.o.y, b.o.z, ns.x);
+    obb[4 * (int64_t)i + 1] = make_float4(b.a1.x, b.a1.y, b.a1.z, ns.y);
+    obb[4 * (int64_t)i + 2] = make_float4(b.a2.x, b.a2.y, b.a2.z, ns.z);
+    obb[4 * (int64_t)i + 3] = make_float4(b.e.x, b.e.y, b.e.z, 0.f);
+}
+
+__device__ __forceinline__ Obb load_obb(const float4* obb, int i, float3* ns) {
+    const float4 p = __ldcg(obb + 4 * (int64_t)i), q = __ldcg(obb + 4 * (int64_t)i + 1);
+    const float4 u = __ldcg(obb + 4 * (int64_t)i + 2), w = __ldcg(obb + 4 * (int64_t)i + 3);
+    Obb b;
+    b.o = make_float3(p.x, p.y, p.z);
+    b.a1 = make_float3(q.x, q.y, q.z);
+    b.a2 = make_float3(u.x, u.y, u.z);
+    b.e = make_float3(w.x, w.y, w.z);
+    *ns = make_float3(p.w, q.w, u.w);
+    return b;
+}
+
+// Boxes of the internal nodes whose subtree holds at most OBB_EXACT
+// triangles, one warp per node: the lanes stride over the node's sorted
+// triangles for the normal sum, then for the extents (butterfly reductions,
+// so every lane holds the same frame).
+constexpr int OBB_WARPS = 4;
+
+__global__ void __launch_bounds__(OBB_WARPS * 32) k_obb_exact(const int2* __restrict__ range, int n,
+                                                              const float4* __restrict__ tris,
+                                                              float4* __restrict__ obb) {
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * OBB_WARPS + (threadIdx.x >> 5);
+    if (i >= n - 1) return;  // warp-uniform
+    const int2 r = range[i];
+    if (r.y - r.x + 1 > OBB_EXACT) return;
+    const unsigned FULL = 0xffffffffu;
+    float3 ns = make_float3(0.f, 0.f, 0.f), v[3], nn, edge;
+    for (int k = r.x + lane; k <= r.y; k += 32) {
+        rec_tri(tris, k, v, &nn, &edge);
+        ns.x += nn.x; ns.y += nn.y; ns.z += nn.z;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        ns.x += __shfl_xor_sync(FULL, ns.x, o);
+        ns.y += __shfl_xor_sync(FULL, ns.y, o);
+        ns.z += __shfl_xor_sync(FULL, ns.z, o);
+    }
+    float3 a1, a2;
+    obb_frame(ns, make_float3(NAN, NAN, NAN), a1, a2);
+    const float3 a3 = obb_a3(a1, a2);
+    rec_tri(tris, r.x, v, &nn, &edge);
+    const float3 ref = v[0];
+    Ext x;
+    x.init();
+    for (int k = r.x + lane; k <= r.y; k += 32) {
+        rec_tri(tris, k, v, &nn, &edge);
+        for (int c = 0; c < 3; ++c) x.add(a1, a2, a3, ref, v[c].x, v[c].y, v[c].z);
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        for (int d = 0; d < 3; ++d) {
+            x.lo[d] = fminf(x.lo[d], __shfl_xor_sync(FULL, x.lo[d], o));
+            x.hi[d] = fmaxf(x.hi[d], __shfl_xor_sync(FULL, x.hi[d], o));
+        }
+    if (lane == 0) store_obb(obb, i, x.finish(a1, a2, a3, ref), ns);
+}
+
+__device__ void add_corners(Ext& x, float3 a1, float3 a2, float3 a3, float3 r, const Obb& c) {
+    const float3 c3 = obb_a3(c.a1, c.a2);
+    for (int m = 0; m < 8; ++m) {
+        const float t1 = (m & 1) ? c.e.x : 0.f, t2 = (m & 2) ? c.e.y : 0.f, t3 = (m & 4) ? c.e.z : 0.f;
+        x.add(a1, a2, a3, r, c.o.x + t1 * c.a1.x + t2 * c.a2.x + t3 * c3.x,
+              c.o.y + t1 * c.a1.y + t2 * c.a2.y + t3 * c3.y, c.o.z + t1 * c.a1.z + t2 * c.a2.z + t3 * c3.z);
+    }
+}
+
+// Boxes of the larger nodes, bottom-up: the second thread to reach a node
+// merges its children (normal sums; extents from the children's corners).
+__global__ void k_obb_walk(const float4* __restrict__ nodes, const int2* __restrict__ range, int n,
+                           const int* __restrict__ parent, int* flags, const float4* __restrict__ tris,
+                           float4* obb, int* status) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    int slot = (n - 1) + j;
+    for (int level = 0;; ++level) {
+        if (level > 128) {
+            atomicOr(status, 4);
+            return;
+        }
+        const int ps = parent[slot];
+        if (ps < 0) return;  // root done
+        const int p = ps >> 1;
+        __threadfence();
+        if (atomicAdd(&flags[p], 1) == 0) return;
+        __threadfence();
+        const int2 r = range[p];
+        if (r.y - r.x + 1 > OBB_EXACT) {
+            Obb cb[2];
+            float3 cn[2];
+            for (int side = 0; side < 2; ++side) {
+                const int c = __float_as_int(__ldcg(&nodes[4 * (int64_t)p + side].w));
+                if (c < 0) cb[side] = obb_of_tri(tris, ~c, &cn[side]);
+                else cb[side] = load_obb(obb, c, &cn[side]);
+            }
+            const float3 ns = make_float3(cn[0].x + cn[1].x, cn[0].y + cn[1].y, cn[0].z + cn[1].z);
+            float3 a1, a2;
+            obb_frame(ns, make_float3(NAN, NAN, NAN), a1, a2);
+            const float3 a3 = obb_a3(a1, a2);
+            Ext x;
+            x.init();
+            add_corners(x, a1, a2, a3, cb[0].o, cb[0]);
+            add_corners(x, a1, a2, a3, cb[0].o, cb[1]);
+            store_obb(obb, p, x.finish(a1, a2, a3, cb[0].o), ns);
+        }
+        slot = p;
+    }
+}
+
+// Traversal records, 8 float4 per internal node, per child (left then right):
+//   (o.xyz, id) (a1.xyz, count) (a2.xyz, e.x) (e.y, e.z, 0, 0)
+// id >= 0 an internal node, ~first for a bucket of `count` (1..DF_BUCKET)
+// sorted triangles.
+__global__ void k_obb_nodes(const float4* __restrict__ nodes, const int2* __restrict__ range, int n,
+                            const float4* __restrict__ tris, const float4* __restrict__ obb,
+                            float4* __restrict__ tnodes) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
-    float4* nd = nodes + 4 * (int64_t)i;
     for (int side = 0; side < 2; ++side) {
-        const int c = __float_as_int(nd[side].w);
+        const int c = __float_as_int(nodes[4 * (int64_t)i + side].w);
         int id = c, cnt = 0;
+        Obb b;
+        float3 ns;
         if (c < 0) {
             cnt = 1;
+            b = obb_of_tri(tris, ~c, &ns);
         } else {
             const int2 r = range[c];
-            if (r.y - r.x + 1 <= k) {
+            b = load_obb(obb, c, &ns);
+            if (r.y - r.x + 1 <= DF_BUCKET) {
                 id = ~r.x;
                 cnt = r.y - r.x + 1;
             }
         }
-        nd[side].w = __int_as_float(id);
-        nd[2 + side].w = __int_as_float(cnt);
+        float4* t = tnodes + 8 * (int64_t)i + 4 * side;
+        t[0] = make_float4(b.o.x, b.o.y, b.o.z, __int_as_float(id));
+        t[1] = make_float4(b.a1.x, b.a1.y, b.a1.z, __int_as_float(cnt));
+        t[2] = make_float4(b.a2.x, b.a2.y, b.a2.z, b.e.x);
+        t[3] = make_float4(b.e.y, b.e.z, 0.f, 0.f);
     }
+}
+
+// Squared distance from p to a child's box (the bound the traversal uses).
+__device__ __forceinline__ float obb_d2(float px, float py, float pz, float4 g0, float4 g1, float4 g2, float4 g3) {
+    const float qx = __fsub_rn(px, g0.x), qy = __fsub_rn(py, g0.y), qz = __fsub_rn(pz, g0.z);
+    const float3 a1 = make_float3(g1.x, g1.y, g1.z), a2 = make_float3(g2.x, g2.y, g2.z);
+    const float3 a3 = obb_a3(a1, a2);
+    const float t1 = dotf3(a1, qx, qy, qz), t2 = dotf3(a2, qx, qy, qz), t3 = dotf3(a3, qx, qy, qz);
+    const float s1 = fmaxf(fmaxf(-t1, t1 - g2.w), 0.f);
+    const float s2 = fmaxf(fmaxf(-t2, t2 - g3.x), 0.f);
+    const float s3 = fmaxf(fmaxf(-t3, t3 - g3.y), 0.f);
+    return s1 * s1 + s2 * s2 + s3 * s3;
 }
 
 // ---------------------------------------------------------------------------
@@ -386,12 +641,6 @@ constexpr float kSlack = 2e-6f;
 __device__ __forceinline__ float slack_bound(float best) { return best + kSlack * (2.f * sqrtf(best) + kSlack); }
 constexpr int TRAV_STACK = 64;
 
-__device__ __forceinline__ float box_d2(float px, float py, float pz, float4 lo, float4 hi) {
-    const float dx = fmaxf(fmaxf(lo.x - px, px - hi.x), 0.f);
-    const float dy = fmaxf(fmaxf(lo.y - py, py - hi.y), 0.f);
-    const float dz = fmaxf(fmaxf(lo.z - pz, pz - hi.z), 0.f);
-    return dx * dx + dy * dy + dz * dz;
-}
 
 // Packet shapes (voxels per warp along x, y, z; product 32), selectable per
 // launch: MO_PACKET_4x4x2 (default), 8x4x1, 4x2x4, 2x4x4, 8x2x2.
@@ -441,11 +690,12 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) k_df_lbvh(const float4* __res
                 if (lane == 0) atomicOr(status, 4);
                 break;
             }
-            const float4* nd = nodes + 4 * (int64_t)node;
-            const float4 a = __ldg(nd), b = __ldg(nd + 1), c = __ldg(nd + 2), d = __ldg(nd + 3);
-            const int L = __float_as_int(a.w), R = __float_as_int(b.w);
-            const int cl = __float_as_int(c.w), cr = __float_as_int(d.w);  // bucket sizes (0: internal)
-            const float dl = box_d2(px, py, pz, a, b), dr = box_d2(px, py, pz, c, d);
+            const float4* nd = nodes + 8 * (int64_t)node;
+            const float4 l0 = __ldg(nd), l1 = __ldg(nd + 1), l2 = __ldg(nd + 2), l3 = __ldg(nd + 3);
+            const float4 r0 = __ldg(nd + 4), r1 = __ldg(nd + 5), r2 = __ldg(nd + 6), r3 = __ldg(nd + 7);
+            const int L = __float_as_int(l0.w), R = __float_as_int(r0.w);
+            const int cl = __float_as_int(l1.w), cr = __float_as_int(r1.w);  // bucket sizes (0: internal)
+            const float dl = obb_d2(px, py, pz, l0, l1, l2, l3), dr = obb_d2(px, py, pz, r0, r1, r2, r3);
             bool wl = __any_sync(FULL, dl < lim);
             bool wr = __any_sync(FULL, dr < lim);
             // the opened buckets' triangles, left then right, one test body
@@ -550,7 +800,9 @@ struct BuildScratch {
     int* hist;
     float* rootbox;
     int* status;
-    int2* range;  // leaves [first, last] of every internal node
+    int2* range;    // leaves [first, last] of every internal node
+    float4* obb;    // 4 float4 per internal node: its oriented box and normal sum
+    float4* tnodes; // 8 float4 per internal node: the traversal records
     size_t bytes;
 };
 
@@ -579,6 +831,8 @@ static BuildScratch plan_scratch(char* base, int64_t nv, int64_t nf, int method)
         s.flags = reinterpret_cast<int*>(take(sizeof(int) * (size_t)nf));
         s.hist = reinterpret_cast<int*>(take(sizeof(int) * radix_hist_ints((int)nf)));
         s.range = reinterpret_cast<int2*>(take(sizeof(int2) * (size_t)(nf > 1 ? nf - 1 : 1)));
+        s.obb = reinterpret_cast<float4*>(take(sizeof(float4) * 4 * (size_t)(nf > 1 ? nf - 1 : 1)));
+        s.tnodes = reinterpret_cast<float4*>(take(sizeof(float4) * 8 * (size_t)(nf > 1 ? nf - 1 : 1)));
     } else {
         s.codes_a = s.codes_b = nullptr;
         s.ids_a = s.ids_b = nullptr;
@@ -586,6 +840,7 @@ static BuildScratch plan_scratch(char* base, int64_t nv, int64_t nf, int method)
         s.boxes = nullptr;
         s.parent = s.flags = s.hist = nullptr;
         s.range = nullptr;
+        s.obb = s.tnodes = nullptr;
     }
     s.bytes = o;
     return s;
@@ -695,10 +950,16 @@ extern "C" int mo_df_build_ex(const float* V, int64_t nv, const int32_t* F, int6
             if (nf > 1) {
                 k_karras<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.codes_a, (int)nf, S.nodes, S.parent, S.flags, S.range);
                 ::mo::note_launch();
-                k_refit<<<ceil_div(nf, 256), 256, 0, s>>>(S.boxes, (int)nf, S.nodes, S.parent, S.flags, S.rootbox, st); ::mo::note_launch();
-                k_buckets<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.nodes, S.range, (int)nf, DF_BUCKET); ::mo::note_launch();
+                k_obb_exact<<<ceil_div(nf - 1, OBB_WARPS), OBB_WARPS * 32, 0, s>>>(S.range, (int)nf, S.tris, S.obb);
+                ::mo::note_launch();
+                k_obb_walk<<<ceil_div(nf, 256), 256, 0, s>>>(S.nodes, S.range, (int)nf, S.parent, S.flags, S.tris,
+                                                             S.obb, st);
+                ::mo::note_launch();
+                k_obb_nodes<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.nodes, S.range, (int)nf, S.tris, S.obb,
+                                                                  S.tnodes);
+                ::mo::note_launch();
             }
-            launch_df_lbvh(packet, S.nodes, S.tris, (int)nf, N, band, band2, grid_out, st, s);
+            launch_df_lbvh(packet, S.tnodes, S.tris, (int)nf, N, band, band2, grid_out, st, s);
         }
         e = cudaGetLastError();
         if (e != cudaSuccess) { fail(e, "df build kernels"); break; }
