@@ -62,6 +62,7 @@ def parse():
     ap.add_argument("--cpu-sample-s", type=float, default=20.0)
     ap.add_argument("--no-extras", action="store_true", help="skip latency/plain/cpu legs")
     ap.add_argument("--no-autotune", action="store_true", help="fixed kernel choices instead of tuned ones")
+    ap.add_argument("--step-grid", type=int, default=0, help="CTAs per fused-step launch (0: all resident)")
     ap.add_argument("--build-streams", type=int, default=6)
     ap.add_argument("--max-building", type=int, default=16)
     ap.add_argument("--engine", default="native", choices=["native", "python"],
@@ -539,7 +540,8 @@ def ours_arm(args, world, rank):
         if args.engine == "native":
             return pool.NativePool(device=dev, group_steps=args.group_steps, results_to_host=results_to_host,
                                    autotuner=tuner, max_pairs=max_pairs, hbm_budget_bytes=budget,
-                                   build_streams=args.build_streams, max_building=args.max_building)
+                                   build_streams=args.build_streams, max_building=args.max_building,
+                                   step_grid=args.step_grid)
         return serving.ServingEngine(device=dev, group_steps=args.group_steps, results_to_host=results_to_host,
                                      autotuner=tuner, max_pairs=max_pairs, hbm_budget_bytes=budget,
                                      build_streams=args.build_streams, max_building=args.max_building)
@@ -682,6 +684,7 @@ def ours_arm(args, world, rank):
                    "group_steps": args.group_steps, "parallelism": "replicas" if world > 1 else "single",
                    "engine": "mo_pool (C ABI)" if args.engine == "native" else "python",
                    "build_streams": args.build_streams, "max_building": args.max_building,
+                   "step_grid": args.step_grid,
                    "l2": "inputs larger than L2 (~1.3 GB meshes, ~20 GB grids per stream)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "kernel": "k_fused_step", "achieved": achieved_ss, "peak": peak,

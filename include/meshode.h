@@ -297,6 +297,9 @@ typedef struct MoPoolConfig {
     int32_t build_streams;     /* 0: 2 */
     int32_t layout;            /* default grid layout (MO_LAYOUT_*) */
     int32_t slices_per_tile;   /* default tile width, 1..8 (0: 8) */
+    int32_t step_grid;         /* CTAs per fused-step launch (0: every resident CTA); fewer
+                                * leave room on the SMs for concurrent DF builds */
+    int32_t reserved;          /* 0 */
 } MoPoolConfig;
 
 typedef struct MoRequest {

@@ -50,7 +50,7 @@ class MoPoolConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_pairs", ctypes.c_int32),
                 ("max_tiles", ctypes.c_int32), ("group_steps", ctypes.c_int32), ("use_graph", ctypes.c_int32),
                 ("max_building", ctypes.c_int32), ("build_streams", ctypes.c_int32), ("layout", ctypes.c_int32),
-                ("slices_per_tile", ctypes.c_int32)]
+                ("slices_per_tile", ctypes.c_int32), ("step_grid", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class MoRequest(ctypes.Structure):

@@ -362,7 +362,7 @@ int upload(MoPool* P) {
 int launch_steps(MoPool* P) {
     void* sv = reinterpret_cast<void*>(P->step);
     for (int k = 0; k < P->cfg.group_steps; ++k) {
-        int rc = mo_fused_step(P->pairs_dev, P->tiles_dev, P->ntiles_dev, P->cfg.max_tiles, k, P->tile_loss, 0, sv);
+        int rc = mo_fused_step(P->pairs_dev, P->tiles_dev, P->ntiles_dev, P->cfg.max_tiles, k, P->tile_loss, P->cfg.step_grid, sv);
         if (rc) return rc;
     }
     return MO_OK;

@@ -20,7 +20,7 @@ from ._lib import check
 class NativePool:
     def __init__(self, device=None, hbm_budget_bytes=None, max_pairs=512, max_tiles=None, group_steps=25,
                  layout=L.MO_LAYOUT_CELL, use_graph=True, max_building=16, results_to_host=True, build_streams=6,
-                 slices_per_tile=L.MO_TILE_WARPS, autotuner=None, df_band=-1.0):
+                 slices_per_tile=L.MO_TILE_WARPS, autotuner=None, df_band=-1.0, step_grid=0):
         L.require_cuda()
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
         self.lib = L.lib()
@@ -28,7 +28,7 @@ class NativePool:
             hbm_budget_bytes=int(hbm_budget_bytes or 0), max_pairs=int(max_pairs),
             max_tiles=int(max_tiles if max_tiles is not None else 1 << 17), group_steps=int(group_steps),
             use_graph=1 if use_graph else 0, max_building=int(max_building), build_streams=int(build_streams),
-            layout=int(layout), slices_per_tile=int(slices_per_tile))
+            layout=int(layout), slices_per_tile=int(slices_per_tile), step_grid=int(step_grid))
         self.S = int(group_steps)
         self.layout = int(layout)
         self.autotuner = autotuner
