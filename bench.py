@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip latency/plain/cpu legs")
     ap.add_argument("--no-autotune", action="store_true", help="fixed kernel choices instead of tuned ones")
     ap.add_argument("--step-grid", type=int, default=0, help="CTAs per fused-step launch (0: all resident)")
+    ap.add_argument("--df-mode", default="full", choices=["on-demand", "full"],
+                    help="grids filled cell by cell as vertices reach them, or built whole at admission")
     ap.add_argument("--build-streams", type=int, default=6)
     ap.add_argument("--max-building", type=int, default=16)
     ap.add_argument("--engine", default="native", choices=["native", "python"],
@@ -536,12 +538,14 @@ def ours_arm(args, world, rank):
     # caching allocator keeps them for the Python engine)
     budget = int(torch.cuda.mem_get_info(dev)[0] * 0.6)
 
-    def make_engine(results_to_host, max_pairs=512):
+    df_mode = L.MO_DF_ON_DEMAND if args.df_mode == "on-demand" else L.MO_DF_FULL
+
+    def make_engine(results_to_host, max_pairs=512, mode=None):
         if args.engine == "native":
             return pool.NativePool(device=dev, group_steps=args.group_steps, results_to_host=results_to_host,
                                    autotuner=tuner, max_pairs=max_pairs, hbm_budget_bytes=budget,
                                    build_streams=args.build_streams, max_building=args.max_building,
-                                   step_grid=args.step_grid)
+                                   step_grid=args.step_grid, df_mode=df_mode if mode is None else mode)
         return serving.ServingEngine(device=dev, group_steps=args.group_steps, results_to_host=results_to_host,
                                      autotuner=tuner, max_pairs=max_pairs, hbm_budget_bytes=budget,
                                      build_streams=args.build_streams, max_building=args.max_building)
@@ -610,6 +614,24 @@ def ours_arm(args, world, rank):
                                 "p99": float(np.percentile(lats, 99)), "arrivals": "poisson 200 req/s"}
         extras["saturated_latency_ms_p99"] = float(np.percentile(
             np.asarray([r.latency for r in last]) * 1e3, 99))
+        if args.engine == "native" and df_mode == L.MO_DF_ON_DEMAND:
+            # the same stream with every grid built whole at admission: its
+            # throughput, and the results compared bit for bit
+            full_eng = make_engine(False, mode=L.MO_DF_FULL)
+            full_eng.run(fresh(req_dev))
+            torch.cuda.synchronize()
+            f0 = torch.cuda.Event(enable_timing=True)
+            f1 = torch.cuda.Event(enable_timing=True)
+            f0.record()
+            full_reqs = fresh(req_dev)
+            full_eng.run(full_reqs)
+            f1.record()
+            torch.cuda.synchronize()
+            full_eng.close()
+            same = all(torch.equal(a.out, b.out) and a.loss == b.loss for a, b in zip(last, full_reqs))
+            extras["full_grid"] = {"value": args.requests / (f0.elapsed_time(f1) * 1e-3), "unit": UNIT,
+                                   "results_bitexact_vs_on_demand": bool(same),
+                                   "note": "every grid built whole at admission (one timed pass)"}
         # plain one-pair-at-a-time GPU loop on a bounded sample
         ids = list(range(min(args.plain_sample, len(specs))))
         t_plain, plain_out = run_plain_gpu(specs, meshes, ids)
@@ -665,7 +687,8 @@ def ours_arm(args, world, rank):
     ss_reqs = fresh(req_dev)
     for r in ss_reqs:
         r.steps = 100000
-    ss_engine = make_engine(False, max_pairs=len(ss_reqs) + 1)
+    # full grids here: the groups time the fused step alone, with no fills
+    ss_engine = make_engine(False, max_pairs=len(ss_reqs) + 1, mode=L.MO_DF_FULL)
     if args.engine == "native":
         engine.close()
         t_ss, bytes_ss, nv_ss = ss_engine.steady_state(ss_reqs, groups=2)
@@ -685,11 +708,17 @@ def ours_arm(args, world, rank):
                    "engine": "mo_pool (C ABI)" if args.engine == "native" else "python",
                    "build_streams": args.build_streams, "max_building": args.max_building,
                    "step_grid": args.step_grid,
+                   "df": ("on-demand cells (traversal tree at admission, a cell's corners when a vertex "
+                          "first reaches it)" if df_mode == L.MO_DF_ON_DEMAND else "full grid at admission"),
                    "l2": "inputs larger than L2 (~1.3 GB meshes, ~20 GB grids per stream)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "kernel": "k_fused_step", "achieved": achieved_ss, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved_ss / peak,
                      "traffic": (TRAFFIC_BYTES_PER_VERTEX * nv_ss) if TRAFFIC_BYTES_PER_VERTEX else None,
+                     # measured DRAM bytes over the launch time: the neighbour
+                     # gathers the formula counts are mostly served from L1/L2
+                     "traffic_gbs": TRAFFIC_BYTES_PER_VERTEX * nv_ss / t_ss / 1e9,
+                     "traffic_frac": TRAFFIC_BYTES_PER_VERTEX * nv_ss / t_ss / 1e9 / peak,
                      "algorithmic_bytes_per_launch": bytes_ss, "ms_per_launch": t_ss * 1e3,
                      "launch": "all %d pairs of the stream active (%d vertices)" % (len(ss_reqs), nv_ss),
                      "bytes_formula": "104*V + 44*H per pair-step",

@@ -137,6 +137,16 @@ int mo_df_build_ex(const float* V, int64_t nv, const int32_t* F, int64_t nf, int
  * band: its losses and results are bit-identical to an exact grid's, and the
  * build skips most of the far field. */
 float mo_df_loss_band(int N);
+/* The target's traversal tree alone, for on-demand fills (mo_df_lazy_fill):
+ * the steps of the LBVH build of mo_df_build_ex without the grid pass.
+ * tree_out (mo_df_tree_bytes(nf) bytes, 16-byte aligned) gets the sorted
+ * triangle records, then the internal nodes' traversal records.  scratch:
+ * mo_df_tree_scratch_bytes; status_out (device int32) gets bit 1 for a face
+ * index out of range.  Nothing is synchronised. */
+size_t mo_df_tree_bytes(int64_t nf);
+size_t mo_df_tree_scratch_bytes(int64_t nv, int64_t nf);
+int mo_df_tree_build(const float* V, int64_t nv, const int32_t* F, int64_t nf, const double* params4,
+                     void* scratch, size_t scratch_bytes, void* tree_out, int32_t* status_out, void* stream);
 /* Method MO_DF_AUTO resolves to (host-side heuristic, exported for tests). */
 int mo_df_method_for(int64_t nf, int N);
 
@@ -246,6 +256,27 @@ typedef struct MoPair {
     int32_t t0;             /* steps completed before this group of launches */
     int32_t t_end;          /* last step to run */
     int32_t tile0, ntiles;  /* the pair's contiguous range in the MoTile array */
+    /* On-demand distance field (df_cells != NULL, MO_LAYOUT_CELL only): a
+     * cell of `grid` is written by mo_df_lazy_fill before any step reads it.
+     * A step that moves a vertex into a cell whose bit is not yet set sets
+     * it and queues the cell (df_queue), and queues every voxel packet the
+     * cell's corners lie in whose bit is not yet set (df_pqueue); counters
+     * df_queue_count[2k] (cells) and [2k+1] (packets) for launch index k.
+     * The fill launched after that step computes the packets, then writes
+     * the cells, so the next step finds them.  Every voxel value is the one
+     * mo_df_build_ex stores. */
+    const float* df_tree;      /* mo_df_tree_build output */
+    float* df_lin;             /* float [N^3]: the voxel values computed so far */
+    uint32_t* df_cells;        /* bit per cell ((N-1)^3): queued, then written */
+    uint32_t* df_packets;      /* bit per 4x4x2 voxel packet: queued, then computed */
+    int32_t* df_status;        /* bit 2: traversal stack overflow, 4: malformed tree, 8: queue full */
+    int32_t* df_queue;         /* (pair index, cell) int32 pairs, df_queue_cap of them */
+    int32_t* df_pqueue;        /* (pair index, packet) int32 pairs, 8 * df_queue_cap of them */
+    int32_t* df_queue_count;   /* two counters per launch of the group */
+    int32_t df_ntri;           /* target triangles */
+    int32_t df_queue_cap;
+    float df_band;             /* the build band (mo_df_loss_band(N)) */
+    int32_t df_pad;
 } MoPair;
 
 typedef struct MoTile {
@@ -269,6 +300,20 @@ int mo_fused_step(const MoPair* pairs, const MoTile* tiles, const int32_t* ntile
  * positions before step t0+k+1. */
 int mo_pair_loss(const MoPair* pairs, int npairs, int max_tiles, int nlaunch, const float* tile_loss,
                  double* pair_loss, void* stream);
+/* On-demand distance field.  mo_df_lazy_bytes(N): the two bit sets of a
+ * pair (cells, then packets; zero them before first use).  mo_df_lazy_seed
+ * queues the cells of nv float4 positions (pair index `pair` of `pairs`)
+ * and their packets, as a step does: cells into queue (cap entries),
+ * packets into pqueue (8 * cap entries), counts[0] / counts[1] counting
+ * them.  mo_df_lazy_fill computes the queued packets, then writes the
+ * queued cells.  Both read the pair table from device memory.  Grids up to
+ * MO_DF_LAZY_MAX_N per axis (df_status bit 16 above it). */
+#define MO_DF_LAZY_MAX_N 1024
+size_t mo_df_lazy_bytes(int N);
+int mo_df_lazy_seed(const MoPair* pairs, int pair, const float* pos4, int64_t nv, int32_t* queue,
+                    int32_t* pqueue, int32_t* counts, int cap, void* stream);
+int mo_df_lazy_fill(const MoPair* pairs, const int32_t* queue, const int32_t* pqueue, const int32_t* counts,
+                    int cap, void* stream);
 
 /* ------------------------------------------------------------------------
  * Serving pool: admit / step / retire deformation requests.  A request is one
@@ -299,8 +344,12 @@ typedef struct MoPoolConfig {
     int32_t slices_per_tile;   /* default tile width, 1..8 (0: 8) */
     int32_t step_grid;         /* CTAs per fused-step launch (0: every resident CTA); fewer
                                 * leave room on the SMs for concurrent DF builds */
-    int32_t reserved;          /* 0 */
+    int32_t df_mode;           /* MO_DF_FULL: build every grid cell at admission;
+                                * MO_DF_ON_DEMAND: build the traversal tree at admission and
+                                * each cell when a vertex first reaches it (same values) */
 } MoPoolConfig;
+#define MO_DF_FULL 0
+#define MO_DF_ON_DEMAND 1
 
 typedef struct MoRequest {
     const float* srcV;   /* [nv,3] raw source vertices */
@@ -337,7 +386,7 @@ typedef struct MoPoolStats {
     uint64_t peak_bytes;
     int32_t queued, building, active, retiring;
     int32_t active_tiles;
-    int32_t pad;
+    int32_t fill_launches_per_step; /* kernels of the on-demand fill after each fused step (0: full grids) */
 } MoPoolStats;
 
 int mo_pool_create(const MoPoolConfig* cfg, MoPool** pool_out);

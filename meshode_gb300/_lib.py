@@ -18,6 +18,8 @@ MO_DF_AUTO, MO_DF_BRUTE, MO_DF_LBVH = 0, 1, 2
 MO_EDGES_FACES, MO_EDGES_LIST = 0, 1
 MO_TILE_WARPS = 8
 MO_REQ_FAILED, MO_REQ_QUEUED, MO_REQ_BUILDING, MO_REQ_ACTIVE, MO_REQ_DONE = -1, 0, 1, 2, 3
+MO_DF_FULL, MO_DF_ON_DEMAND = 0, 1
+MO_DF_LAZY_MAX_N = 1024
 
 _P = ctypes.c_void_p
 _I = ctypes.c_int
@@ -34,6 +36,9 @@ class MoPair(ctypes.Structure):
         ("w_edge", _F), ("mask_thresh", _F), ("use_mask", ctypes.c_int32), ("grad_scale", _F),
         ("one_minus_b1", _F), ("b2", _F), ("one_minus_b2", _F), ("eps", _F),
         ("t0", ctypes.c_int32), ("t_end", ctypes.c_int32), ("tile0", ctypes.c_int32), ("ntiles", ctypes.c_int32),
+        ("df_tree", _P), ("df_lin", _P), ("df_cells", _P), ("df_packets", _P), ("df_status", _P),
+        ("df_queue", _P), ("df_pqueue", _P), ("df_queue_count", _P), ("df_ntri", ctypes.c_int32), ("df_queue_cap", ctypes.c_int32),
+        ("df_band", _F), ("df_pad", ctypes.c_int32),
     ]
 
 
@@ -50,7 +55,7 @@ class MoPoolConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_pairs", ctypes.c_int32),
                 ("max_tiles", ctypes.c_int32), ("group_steps", ctypes.c_int32), ("use_graph", ctypes.c_int32),
                 ("max_building", ctypes.c_int32), ("build_streams", ctypes.c_int32), ("layout", ctypes.c_int32),
-                ("slices_per_tile", ctypes.c_int32), ("step_grid", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("slices_per_tile", ctypes.c_int32), ("step_grid", ctypes.c_int32), ("df_mode", ctypes.c_int32)]
 
 
 class MoRequest(ctypes.Structure):
@@ -66,7 +71,8 @@ class MoPoolStats(ctypes.Structure):
     _fields_ = [("submitted", _I64), ("done", _I64), ("failed", _I64), ("groups", _I64),
                 ("fused_launches", _I64), ("bytes_in_use", ctypes.c_uint64), ("peak_bytes", ctypes.c_uint64),
                 ("queued", ctypes.c_int32), ("building", ctypes.c_int32), ("active", ctypes.c_int32),
-                ("retiring", ctypes.c_int32), ("active_tiles", ctypes.c_int32), ("pad", ctypes.c_int32)]
+                ("retiring", ctypes.c_int32), ("active_tiles", ctypes.c_int32),
+                ("fill_launches_per_step", ctypes.c_int32)]
 
 
 # name -> (restype, argtypes)
@@ -84,6 +90,12 @@ _SIGS = {
     "mo_df_build_ex": (_I, [_P, _I64, _P, _I64, _I, _P, _P, _P, _SZ, _P, _P, _P]),
     "mo_df_build_noalloc": (_I, [_P, _I64, _P, _I64, _I, _P, _P, _P]),
     "mo_df_noalloc_scratch_capacity": (_SZ, []),
+    "mo_df_tree_bytes": (_SZ, [_I64]),
+    "mo_df_tree_scratch_bytes": (_SZ, [_I64, _I64]),
+    "mo_df_tree_build": (_I, [_P, _I64, _P, _I64, _P, _P, _SZ, _P, _P, _P]),
+    "mo_df_lazy_bytes": (_SZ, [_I]),
+    "mo_df_lazy_seed": (_I, [_P, _I, _P, _I64, _P, _P, _P, _I, _P]),
+    "mo_df_lazy_fill": (_I, [_P, _P, _P, _P, _I, _P]),
     "mo_lbvh_build": (_I, [_P, _I64, _P, _I64, _P, _P, _SZ, _P, _P, _P, _P, _P, _P]),
     "mo_grid_bytes": (_SZ, [_I, _I]),
     "mo_grid_relayout": (_I, [_P, _I, _I, _P, _P]),

@@ -1,0 +1,219 @@
+// Nearest-triangle queries of the distance-field build, shared by the
+// full-grid build (mo_dfbuild.cu) and the on-demand cell fills
+// (mo_lazydf.cu): the triangle records and their exact squared-distance
+// query, the oriented-box bound of a tree child, and the warp-packet walk
+// of the tree that gives one voxel's stored value.
+// Reference: igl::point_mesh_squared_distance as called by
+// Mesh::ConstructDistanceField (src/lib/mesh.cc:106-152).
+#pragma once
+
+#include <cfloat>
+
+#include "mo_common.cuh"
+
+namespace mo {
+
+// ---------------------------------------------------------------------------
+// Triangle records, 5 float4 (80 B), in a per-triangle 2D frame so a query
+// costs a projection and three 2D segment distances:
+//   r0 = (a, bx)  r1 = (ex, cx)  r2 = (ey, cy)  r3 = (n, 1)
+//   r4 = (1/bx, 1/|ac|^2, 1/|bc|^2, cx - bx)
+// with ex = ab/|ab|, n the unit normal, ey = n x ex, and the triangle at
+// A=(0,0), B=(bx,0), C=(cx,cy), cy > 0 in (ex, ey).  A degenerate triangle
+// (zero area or zero-length ab) keeps its vertices instead and is measured
+// by its three segments:
+//   r0 = (a, 0)  r1 = (b, 0)  r2 = (c, 0)  r3 = (0, 0, 0, 0)
+//   r4 = (1/|ab|^2, 1/|bc|^2, 1/|ca|^2, 0)   (0 for a zero-length segment)
+// ---------------------------------------------------------------------------
+struct Tri {
+    float4 r0, r1, r2, r3, r4;
+};
+constexpr int TRI_F4 = 5;
+
+// The query arithmetic is written with explicit fmaf / __fmul_rn / __fadd_rn
+// so that every kernel that inlines it (LBVH traversal, brute force) rounds
+// identically and the two build methods give the same grid bit for bit.
+__device__ __forceinline__ float dot3e(float ax, float ay, float az, float bx, float by, float bz) {
+    return fmaf(az, bz, fmaf(ay, by, __fmul_rn(ax, bx)));
+}
+
+__device__ __forceinline__ float seg3_d2(float px, float py, float pz, float4 a, float4 b, float inv_l2) {
+    const float ex = __fsub_rn(b.x, a.x), ey = __fsub_rn(b.y, a.y), ez = __fsub_rn(b.z, a.z);
+    const float apx = __fsub_rn(px, a.x), apy = __fsub_rn(py, a.y), apz = __fsub_rn(pz, a.z);
+    float t = __fmul_rn(dot3e(apx, apy, apz, ex, ey, ez), inv_l2);
+    t = fminf(fmaxf(t, 0.f), 1.f);
+    const float qx = fmaf(-t, ex, apx), qy = fmaf(-t, ey, apy), qz = fmaf(-t, ez, apz);
+    return dot3e(qx, qy, qz, qx, qy, qz);
+}
+
+// Squared distance from p to the triangle.  `cut` is this lane's current
+// best: when no lane of the (converged) warp can beat its best because the
+// plane distance alone is too large, the in-plane part is skipped and
+// FLT_MAX returned.  The record is warp-uniform, so both branches are too.
+__device__ __forceinline__ float tri_d2(float px, float py, float pz, const Tri& T, float cut) {
+    if (T.r3.w != 0.f) {
+        const float qx = __fsub_rn(px, T.r0.x), qy = __fsub_rn(py, T.r0.y), qz = __fsub_rn(pz, T.r0.z);
+        const float h = dot3e(qx, qy, qz, T.r3.x, T.r3.y, T.r3.z);
+        const float h2 = __fmul_rn(h, h);
+        if (!__any_sync(0xffffffffu, h2 < cut)) return FLT_MAX;
+        const float x = dot3e(qx, qy, qz, T.r1.x, T.r1.y, T.r1.z);
+        const float y = dot3e(qx, qy, qz, T.r2.x, T.r2.y, T.r2.z);
+        const float bx = T.r0.w, cx = T.r1.w, cy = T.r2.w, ebx = T.r4.w;
+        const float y2 = __fmul_rn(y, y);
+        // A-B along the x axis
+        float t = fminf(fmaxf(__fmul_rn(x, T.r4.x), 0.f), 1.f);
+        float dx = fmaf(-t, bx, x);
+        float d = fmaf(dx, dx, y2);
+        // A-C
+        t = fminf(fmaxf(__fmul_rn(fmaf(x, cx, __fmul_rn(y, cy)), T.r4.y), 0.f), 1.f);
+        dx = fmaf(-t, cx, x);
+        float dy = fmaf(-t, cy, y);
+        d = fminf(d, fmaf(dx, dx, __fmul_rn(dy, dy)));
+        // B-C
+        const float xb = __fsub_rn(x, bx);
+        t = fminf(fmaxf(__fmul_rn(fmaf(xb, ebx, __fmul_rn(y, cy)), T.r4.z), 0.f), 1.f);
+        dx = fmaf(-t, ebx, xb);
+        dy = fmaf(-t, cy, y);
+        d = fminf(d, fmaf(dx, dx, __fmul_rn(dy, dy)));
+        // inside: left of A->B, B->C and C->A (counter-clockwise in the frame)
+        const bool inside = (y >= 0.f) && (fmaf(ebx, y, -__fmul_rn(cy, xb)) >= 0.f) &&
+                            (fmaf(cy, x, -__fmul_rn(cx, y)) >= 0.f);
+        return inside ? h2 : __fadd_rn(h2, d);
+    }
+    float d = seg3_d2(px, py, pz, T.r0, T.r1, T.r4.x);
+    d = fminf(d, seg3_d2(px, py, pz, T.r1, T.r2, T.r4.y));
+    d = fminf(d, seg3_d2(px, py, pz, T.r2, T.r0, T.r4.z));
+    return d;
+}
+
+__device__ __forceinline__ Tri load_tri(const float4* __restrict__ tris, int i) {
+    const float4* p = tris + TRI_F4 * (int64_t)i;
+    Tri t;
+    t.r0 = __ldg(p); t.r1 = __ldg(p + 1); t.r2 = __ldg(p + 2); t.r3 = __ldg(p + 3); t.r4 = __ldg(p + 4);
+    return t;
+}
+
+// a3 exactly as the traversal computes it
+__device__ __forceinline__ float3 obb_a3(float3 a1, float3 a2) {
+    return make_float3(__fsub_rn(__fmul_rn(a1.y, a2.z), __fmul_rn(a1.z, a2.y)),
+                       __fsub_rn(__fmul_rn(a1.z, a2.x), __fmul_rn(a1.x, a2.z)),
+                       __fsub_rn(__fmul_rn(a1.x, a2.y), __fmul_rn(a1.y, a2.x)));
+}
+
+__device__ __forceinline__ float dotf3(float3 a, float x, float y, float z) {
+    return fmaf(a.z, z, fmaf(a.y, y, __fmul_rn(a.x, x)));
+}
+
+// Squared distance from p to a child's box (the bound the traversal uses).
+__device__ __forceinline__ float obb_d2(float px, float py, float pz, float4 g0, float4 g1, float4 g2, float4 g3) {
+    const float qx = __fsub_rn(px, g0.x), qy = __fsub_rn(py, g0.y), qz = __fsub_rn(pz, g0.z);
+    const float3 a1 = make_float3(g1.x, g1.y, g1.z), a2 = make_float3(g2.x, g2.y, g2.z);
+    const float3 a3 = obb_a3(a1, a2);
+    const float t1 = dotf3(a1, qx, qy, qz), t2 = dotf3(a2, qx, qy, qz), t3 = dotf3(a3, qx, qy, qz);
+    const float s1 = fmaxf(fmaxf(-t1, t1 - g2.w), 0.f);
+    const float s2 = fmaxf(fmaxf(-t2, t2 - g3.x), 0.f);
+    const float s3 = fmaxf(fmaxf(-t3, t3 - g3.y), 0.f);
+    return s1 * s1 + s2 * s2 + s3 * s3;
+}
+
+// ---------------------------------------------------------------------------
+// Warp-packet traversal: one warp = a 4x4x2 brick of voxels.  The warp walks
+// the tree together (node and triangle loads are warp-uniform broadcasts);
+// a child is visited when any lane's box distance beats that lane's best.
+// ---------------------------------------------------------------------------
+constexpr int TRAV_WARPS = 4;
+constexpr float kSlack = 2e-6f;
+
+// (sqrt(best) + kSlack)^2: the squared-distance bound a box must beat.
+__device__ __forceinline__ float slack_bound(float best) { return best + kSlack * (2.f * sqrtf(best) + kSlack); }
+constexpr int TRAV_STACK = 64;
+
+
+// Packet shapes (voxels per warp along x, y, z; product 32), selectable per
+// launch: MO_PACKET_4x4x2 (default), 8x4x1, 4x2x4, 2x4x4, 8x2x2.
+// Band: with band > 0 a voxel whose distance is not below `band` stores
+// `band` itself, except in the two lowest layers along each axis (x, y or
+// z <= 1), which stay exact everywhere; band2 = band^2 (FLT_MAX for none).
+__device__ __forceinline__ bool exact_layer(int x, int y, int z) { return x <= 1 || y <= 1 || z <= 1; }
+
+// The value the voxel (x, y, z) of this lane stores: its exact distance to
+// the nearest triangle, or `band` when that is not below the band.  All 32
+// lanes of the warp call it together and walk the tree jointly (node and
+// triangle loads are warp-uniform broadcasts); lanes with valid == false
+// only follow.  stack: this warp's TRAV_STACK ints of shared memory.
+__device__ __forceinline__ float df_voxel_value(const float4* __restrict__ nodes, const float4* __restrict__ tris,
+                                                int ntri, int N, float band, float band2, int x, int y, int z,
+                                                bool valid, int* stack, int* __restrict__ status) {
+    const int lane = threadIdx.x & 31;
+    const float Nf = (float)N;
+    const float px = __fdiv_rn((float)x, Nf), py = __fdiv_rn((float)y, Nf), pz = __fdiv_rn((float)z, Nf);
+    const float init = exact_layer(x, y, z) ? FLT_MAX : band2;
+    float best = valid ? init : -1.0f;
+    // Boxes are visited while their fp32 distance is within kSlack (in
+    // distance units) of the lane's best: the rounding of the box bound can
+    // exceed a triangle's computed distance by far less than that, so no
+    // triangle that could lower `best` is skipped and the result is the exact
+    // minimum of the computed distances, whatever the visit order.  Starting
+    // from band^2 instead of FLT_MAX skips what lies beyond the band and keeps
+    // every distance below it.
+    float lim = valid ? (init == FLT_MAX ? FLT_MAX : slack_bound(init)) : -1.0f;
+    const unsigned FULL = 0xffffffffu;
+    if (ntri == 1) {
+        const float t = tri_d2(px, py, pz, load_tri(tris, 0), best);
+        if (valid && t < best) best = t;
+    } else {
+        int sp = 0;
+        int node = 0;
+        // each node is entered at most once per traversal; the cap only
+        // guards against a corrupted tree
+        const int64_t max_iter = 2 * (int64_t)ntri + 64;
+        for (int64_t iter = 0;; ++iter) {
+            if (iter > max_iter) {
+                if (lane == 0) atomicOr(status, 4);
+                break;
+            }
+            const float4* nd = nodes + 8 * (int64_t)node;
+            const float4 l0 = __ldg(nd), l1 = __ldg(nd + 1), l2 = __ldg(nd + 2), l3 = __ldg(nd + 3);
+            const float4 r0 = __ldg(nd + 4), r1 = __ldg(nd + 5), r2 = __ldg(nd + 6), r3 = __ldg(nd + 7);
+            const int L = __float_as_int(l0.w), R = __float_as_int(r0.w);
+            const int cl = __float_as_int(l1.w), cr = __float_as_int(r1.w);  // bucket sizes (0: internal)
+            const float dl = obb_d2(px, py, pz, l0, l1, l2, l3), dr = obb_d2(px, py, pz, r0, r1, r2, r3);
+            bool wl = __any_sync(FULL, dl < lim);
+            bool wr = __any_sync(FULL, dr < lim);
+            // the opened buckets' triangles, left then right, one test body
+            const int nl = wl ? cl : 0, nr = wr ? cr : 0;
+#pragma unroll 1
+            for (int k = 0; k < nl + nr; ++k) {
+                const int tri = k < nl ? ~L + k : ~R + (k - nl);
+                const float t = tri_d2(px, py, pz, load_tri(tris, tri), best);
+                if (valid && t < best) { best = t; lim = slack_bound(best); }
+            }
+            if (cl > 0) wl = false;
+            if (cr > 0) wr = false;
+            if (wl && wr) {
+                const unsigned nearer_l = __ballot_sync(FULL, valid && dl <= dr);
+                const unsigned act = __ballot_sync(FULL, valid);
+                const bool lfirst = 2 * __popc(nearer_l) >= __popc(act);
+                if (sp >= TRAV_STACK) {  // cannot happen for trees of depth <= 64
+                    if (lane == 0) atomicOr(status, 2);
+                    break;
+                }
+                if (lane == 0) stack[sp] = lfirst ? R : L;
+                ++sp;
+                node = lfirst ? L : R;
+            } else if (wl) {
+                node = L;
+            } else if (wr) {
+                node = R;
+            } else {
+                if (sp == 0) break;
+                __syncwarp();
+                node = stack[--sp];
+            }
+            __syncwarp();
+        }
+    }
+    return best < band2 || init == FLT_MAX ? __fsqrt_rn(best) : band;
+}
+
+}  // namespace mo

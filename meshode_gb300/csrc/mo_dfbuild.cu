@@ -11,6 +11,7 @@
 #include <mutex>
 
 #include "mo_common.cuh"
+#include "mo_df_trav.cuh"
 #include "mo_lbvh.cuh"
 
 namespace mo {
@@ -82,22 +83,7 @@ __global__ void k_normalize_copy(const float* __restrict__ V, int64_t n, const d
     out[i] = (float)__ddiv_rn(__dsub_rn((double)V[i], prm[1 + c]), prm[0]);
 }
 
-// ---------------------------------------------------------------------------
-// Triangle records, 5 float4 (80 B), in a per-triangle 2D frame so a query
-// costs a projection and three 2D segment distances:
-//   r0 = (a, bx)  r1 = (ex, cx)  r2 = (ey, cy)  r3 = (n, 1)
-//   r4 = (1/bx, 1/|ac|^2, 1/|bc|^2, cx - bx)
-// with ex = ab/|ab|, n the unit normal, ey = n x ex, and the triangle at
-// A=(0,0), B=(bx,0), C=(cx,cy), cy > 0 in (ex, ey).  A degenerate triangle
-// (zero area or zero-length ab) keeps its vertices instead and is measured
-// by its three segments:
-//   r0 = (a, 0)  r1 = (b, 0)  r2 = (c, 0)  r3 = (0, 0, 0, 0)
-//   r4 = (1/|ab|^2, 1/|bc|^2, 1/|ca|^2, 0)   (0 for a zero-length segment)
-// ---------------------------------------------------------------------------
-struct Tri {
-    float4 r0, r1, r2, r3, r4;
-};
-constexpr int TRI_F4 = 5;
+// Triangle records (the layout is described in mo_df_trav.cuh).
 
 __device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz) {
     return ax * bx + ay * by + az * bz;
@@ -140,69 +126,6 @@ __device__ Tri make_tri(const float* __restrict__ Vn, int i0, int i1, int i2, fl
         t.r4 = make_float4(lab > 0.f ? 1.0f / lab : 0.f, lbc > 0.f ? 1.0f / lbc : 0.f, lca > 0.f ? 1.0f / lca : 0.f,
                            0.f);
     }
-    return t;
-}
-
-// The query arithmetic is written with explicit fmaf / __fmul_rn / __fadd_rn
-// so that every kernel that inlines it (LBVH traversal, brute force) rounds
-// identically and the two build methods give the same grid bit for bit.
-__device__ __forceinline__ float dot3e(float ax, float ay, float az, float bx, float by, float bz) {
-    return fmaf(az, bz, fmaf(ay, by, __fmul_rn(ax, bx)));
-}
-
-__device__ __forceinline__ float seg3_d2(float px, float py, float pz, float4 a, float4 b, float inv_l2) {
-    const float ex = __fsub_rn(b.x, a.x), ey = __fsub_rn(b.y, a.y), ez = __fsub_rn(b.z, a.z);
-    const float apx = __fsub_rn(px, a.x), apy = __fsub_rn(py, a.y), apz = __fsub_rn(pz, a.z);
-    float t = __fmul_rn(dot3e(apx, apy, apz, ex, ey, ez), inv_l2);
-    t = fminf(fmaxf(t, 0.f), 1.f);
-    const float qx = fmaf(-t, ex, apx), qy = fmaf(-t, ey, apy), qz = fmaf(-t, ez, apz);
-    return dot3e(qx, qy, qz, qx, qy, qz);
-}
-
-// Squared distance from p to the triangle.  `cut` is this lane's current
-// best: when no lane of the (converged) warp can beat its best because the
-// plane distance alone is too large, the in-plane part is skipped and
-// FLT_MAX returned.  The record is warp-uniform, so both branches are too.
-__device__ __forceinline__ float tri_d2(float px, float py, float pz, const Tri& T, float cut) {
-    if (T.r3.w != 0.f) {
-        const float qx = __fsub_rn(px, T.r0.x), qy = __fsub_rn(py, T.r0.y), qz = __fsub_rn(pz, T.r0.z);
-        const float h = dot3e(qx, qy, qz, T.r3.x, T.r3.y, T.r3.z);
-        const float h2 = __fmul_rn(h, h);
-        if (!__any_sync(0xffffffffu, h2 < cut)) return FLT_MAX;
-        const float x = dot3e(qx, qy, qz, T.r1.x, T.r1.y, T.r1.z);
-        const float y = dot3e(qx, qy, qz, T.r2.x, T.r2.y, T.r2.z);
-        const float bx = T.r0.w, cx = T.r1.w, cy = T.r2.w, ebx = T.r4.w;
-        const float y2 = __fmul_rn(y, y);
-        // A-B along the x axis
-        float t = fminf(fmaxf(__fmul_rn(x, T.r4.x), 0.f), 1.f);
-        float dx = fmaf(-t, bx, x);
-        float d = fmaf(dx, dx, y2);
-        // A-C
-        t = fminf(fmaxf(__fmul_rn(fmaf(x, cx, __fmul_rn(y, cy)), T.r4.y), 0.f), 1.f);
-        dx = fmaf(-t, cx, x);
-        float dy = fmaf(-t, cy, y);
-        d = fminf(d, fmaf(dx, dx, __fmul_rn(dy, dy)));
-        // B-C
-        const float xb = __fsub_rn(x, bx);
-        t = fminf(fmaxf(__fmul_rn(fmaf(xb, ebx, __fmul_rn(y, cy)), T.r4.z), 0.f), 1.f);
-        dx = fmaf(-t, ebx, xb);
-        dy = fmaf(-t, cy, y);
-        d = fminf(d, fmaf(dx, dx, __fmul_rn(dy, dy)));
-        // inside: left of A->B, B->C and C->A (counter-clockwise in the frame)
-        const bool inside = (y >= 0.f) && (fmaf(ebx, y, -__fmul_rn(cy, xb)) >= 0.f) &&
-                            (fmaf(cy, x, -__fmul_rn(cx, y)) >= 0.f);
-        return inside ? h2 : __fadd_rn(h2, d);
-    }
-    float d = seg3_d2(px, py, pz, T.r0, T.r1, T.r4.x);
-    d = fminf(d, seg3_d2(px, py, pz, T.r1, T.r2, T.r4.y));
-    d = fminf(d, seg3_d2(px, py, pz, T.r2, T.r0, T.r4.z));
-    return d;
-}
-
-__device__ __forceinline__ Tri load_tri(const float4* __restrict__ tris, int i) {
-    const float4* p = tris + TRI_F4 * (int64_t)i;
-    Tri t;
-    t.r0 = __ldg(p); t.r1 = __ldg(p + 1); t.r2 = __ldg(p + 2); t.r3 = __ldg(p + 3); t.r4 = __ldg(p + 4);
     return t;
 }
 
@@ -375,17 +298,6 @@ constexpr float OBB_INFL = 2e-6f;
 struct Obb {
     float3 o, a1, a2, e;  // origin, axes (a3 = a1 x a2), extents
 };
-
-// a3 exactly as the traversal computes it
-__device__ __forceinline__ float3 obb_a3(float3 a1, float3 a2) {
-    return make_float3(__fsub_rn(__fmul_rn(a1.y, a2.z), __fmul_rn(a1.z, a2.y)),
-                       __fsub_rn(__fmul_rn(a1.z, a2.x), __fmul_rn(a1.x, a2.z)),
-                       __fsub_rn(__fmul_rn(a1.x, a2.y), __fmul_rn(a1.y, a2.x)));
-}
-
-__device__ __forceinline__ float dotf3(float3 a, float x, float y, float z) {
-    return fmaf(a.z, z, fmaf(a.y, y, __fmul_rn(a.x, x)));
-}
 
 __device__ __forceinline__ float3 unit3f(float3 v, float3 fallback) {
     const float n2 = v.x * v.x + v.y * v.y + v.z * v.z;
@@ -617,38 +529,7 @@ __global__ void k_obb_nodes(const float4* __restrict__ nodes, const int2* __rest
     }
 }
 
-// Squared distance from p to a child's box (the bound the traversal uses).
-__device__ __forceinline__ float obb_d2(float px, float py, float pz, float4 g0, float4 g1, float4 g2, float4 g3) {
-    const float qx = __fsub_rn(px, g0.x), qy = __fsub_rn(py, g0.y), qz = __fsub_rn(pz, g0.z);
-    const float3 a1 = make_float3(g1.x, g1.y, g1.z), a2 = make_float3(g2.x, g2.y, g2.z);
-    const float3 a3 = obb_a3(a1, a2);
-    const float t1 = dotf3(a1, qx, qy, qz), t2 = dotf3(a2, qx, qy, qz), t3 = dotf3(a3, qx, qy, qz);
-    const float s1 = fmaxf(fmaxf(-t1, t1 - g2.w), 0.f);
-    const float s2 = fmaxf(fmaxf(-t2, t2 - g3.x), 0.f);
-    const float s3 = fmaxf(fmaxf(-t3, t3 - g3.y), 0.f);
-    return s1 * s1 + s2 * s2 + s3 * s3;
-}
-
-// ---------------------------------------------------------------------------
-// Warp-packet traversal: one warp = a 4x4x2 brick of voxels.  The warp walks
-// the tree together (node and triangle loads are warp-uniform broadcasts);
-// a child is visited when any lane's box distance beats that lane's best.
-// ---------------------------------------------------------------------------
-constexpr int TRAV_WARPS = 4;
-constexpr float kSlack = 2e-6f;
-
-// (sqrt(best) + kSlack)^2: the squared-distance bound a box must beat.
-__device__ __forceinline__ float slack_bound(float best) { return best + kSlack * (2.f * sqrtf(best) + kSlack); }
-constexpr int TRAV_STACK = 64;
-
-
-// Packet shapes (voxels per warp along x, y, z; product 32), selectable per
-// launch: MO_PACKET_4x4x2 (default), 8x4x1, 4x2x4, 2x4x4, 8x2x2.
-// Band: with band > 0 a voxel whose distance is not below `band` stores
-// `band` itself, except in the two lowest layers along each axis (x, y or
-// z <= 1), which stay exact everywhere; band2 = band^2 (FLT_MAX for none).
-__device__ __forceinline__ bool exact_layer(int x, int y, int z) { return x <= 1 || y <= 1 || z <= 1; }
-
+// The full grid: one warp per packet of PX x PY x PZ voxels.
 template <int PX, int PY, int PZ>
 __global__ void __launch_bounds__(TRAV_WARPS * 32) k_df_lbvh(const float4* __restrict__ nodes,
                                                              const float4* __restrict__ tris, int ntri, int N,
@@ -663,75 +544,8 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) k_df_lbvh(const float4* __res
     const int ix = (int)(brick % bx), iy = (int)((brick / bx) % by), iz = (int)(brick / ((int64_t)bx * by));
     const int x = ix * PX + (lane % PX), y = iy * PY + ((lane / PX) % PY), z = iz * PZ + lane / (PX * PY);
     const bool valid = x < N && y < N && z < N;
-    const float Nf = (float)N;
-    const float px = __fdiv_rn((float)x, Nf), py = __fdiv_rn((float)y, Nf), pz = __fdiv_rn((float)z, Nf);
-    const float init = exact_layer(x, y, z) ? FLT_MAX : band2;
-    float best = valid ? init : -1.0f;
-    // Boxes are visited while their fp32 distance is within kSlack (in
-    // distance units) of the lane's best: the rounding of the box bound can
-    // exceed a triangle's computed distance by far less than that, so no
-    // triangle that could lower `best` is skipped and the result is the exact
-    // minimum of the computed distances, whatever the visit order.  Starting
-    // from band^2 instead of FLT_MAX skips what lies beyond the band and keeps
-    // every distance below it.
-    float lim = valid ? (init == FLT_MAX ? FLT_MAX : slack_bound(init)) : -1.0f;
-    const unsigned FULL = 0xffffffffu;
-    if (ntri == 1) {
-        const float t = tri_d2(px, py, pz, load_tri(tris, 0), best);
-        if (valid && t < best) best = t;
-    } else {
-        int sp = 0;
-        int node = 0;
-        // each node is entered at most once per traversal; the cap only
-        // guards against a corrupted tree
-        const int64_t max_iter = 2 * (int64_t)ntri + 64;
-        for (int64_t iter = 0;; ++iter) {
-            if (iter > max_iter) {
-                if (lane == 0) atomicOr(status, 4);
-                break;
-            }
-            const float4* nd = nodes + 8 * (int64_t)node;
-            const float4 l0 = __ldg(nd), l1 = __ldg(nd + 1), l2 = __ldg(nd + 2), l3 = __ldg(nd + 3);
-            const float4 r0 = __ldg(nd + 4), r1 = __ldg(nd + 5), r2 = __ldg(nd + 6), r3 = __ldg(nd + 7);
-            const int L = __float_as_int(l0.w), R = __float_as_int(r0.w);
-            const int cl = __float_as_int(l1.w), cr = __float_as_int(r1.w);  // bucket sizes (0: internal)
-            const float dl = obb_d2(px, py, pz, l0, l1, l2, l3), dr = obb_d2(px, py, pz, r0, r1, r2, r3);
-            bool wl = __any_sync(FULL, dl < lim);
-            bool wr = __any_sync(FULL, dr < lim);
-            // the opened buckets' triangles, left then right, one test body
-            const int nl = wl ? cl : 0, nr = wr ? cr : 0;
-#pragma unroll 1
-            for (int k = 0; k < nl + nr; ++k) {
-                const int tri = k < nl ? ~L + k : ~R + (k - nl);
-                const float t = tri_d2(px, py, pz, load_tri(tris, tri), best);
-                if (valid && t < best) { best = t; lim = slack_bound(best); }
-            }
-            if (cl > 0) wl = false;
-            if (cr > 0) wr = false;
-            if (wl && wr) {
-                const unsigned nearer_l = __ballot_sync(FULL, valid && dl <= dr);
-                const unsigned act = __ballot_sync(FULL, valid);
-                const bool lfirst = 2 * __popc(nearer_l) >= __popc(act);
-                if (sp >= TRAV_STACK) {  // cannot happen for trees of depth <= 64
-                    if (lane == 0) atomicOr(status, 2);
-                    break;
-                }
-                if (lane == 0) stack[w][sp] = lfirst ? R : L;
-                ++sp;
-                node = lfirst ? L : R;
-            } else if (wl) {
-                node = L;
-            } else if (wr) {
-                node = R;
-            } else {
-                if (sp == 0) break;
-                __syncwarp();
-                node = stack[w][--sp];
-            }
-            __syncwarp();
-        }
-    }
-    if (valid) grid[((int64_t)z * N + y) * N + x] = best < band2 || init == FLT_MAX ? __fsqrt_rn(best) : band;
+    const float v = df_voxel_value(nodes, tris, ntri, N, band, band2, x, y, z, valid, stack[w], status);
+    if (valid) grid[((int64_t)z * N + y) * N + x] = v;
 }
 
 template <int PX, int PY, int PZ>
@@ -846,9 +660,66 @@ static BuildScratch plan_scratch(char* base, int64_t nv, int64_t nf, int method)
     return s;
 }
 
+// The LBVH build up to the traversal inputs (S.tris: sorted triangle
+// records, S.tnodes: node records) from the normalised vertices S.Vn.
+static cudaError_t issue_tree(const BuildScratch& S, const int32_t* F, int64_t nv, int64_t nf, int* st,
+                              cudaStream_t s) {
+    k_morton<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.codes_a, S.ids_a, st); ::mo::note_launch();
+    cudaError_t e = radix_sort_pairs(S.codes_a, S.ids_a, S.codes_b, S.ids_b, (int)nf, 30, S.hist, s);
+    if (e != cudaSuccess) return e;
+    k_tri_records<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.ids_a, S.tris, S.boxes); ::mo::note_launch();
+    if (nf > 1) {
+        k_karras<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.codes_a, (int)nf, S.nodes, S.parent, S.flags, S.range);
+        ::mo::note_launch();
+        k_obb_exact<<<ceil_div(nf - 1, OBB_WARPS), OBB_WARPS * 32, 0, s>>>(S.range, (int)nf, S.tris, S.obb);
+        ::mo::note_launch();
+        k_obb_walk<<<ceil_div(nf, 256), 256, 0, s>>>(S.nodes, S.range, (int)nf, S.parent, S.flags, S.tris, S.obb,
+                                                     st);
+        ::mo::note_launch();
+        k_obb_nodes<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.nodes, S.range, (int)nf, S.tris, S.obb, S.tnodes);
+        ::mo::note_launch();
+    }
+    return cudaGetLastError();
+}
+
 }  // namespace mo
 
 using namespace mo;
+
+extern "C" size_t mo_df_tree_bytes(int64_t nf) {
+    if (nf <= 0) return 0;
+    return sizeof(float4) * ((size_t)TRI_F4 * nf + 8 * (size_t)(nf > 1 ? nf - 1 : 1));
+}
+
+extern "C" size_t mo_df_tree_scratch_bytes(int64_t nv, int64_t nf) {
+    if (nv < 0 || nf < 0) return 0;
+    return plan_scratch(nullptr, nv, nf, MO_DF_LBVH).bytes;
+}
+
+extern "C" int mo_df_tree_build(const float* V, int64_t nv, const int32_t* F, int64_t nf, const double* params4,
+                                void* scratch, size_t scratch_bytes, void* tree_out, int32_t* status_out,
+                                void* stream) {
+    MO_CHECK_ARG(nv > 0 && nf > 0, "target mesh must have vertices and faces (nv=%lld nf=%lld)", (long long)nv,
+                 (long long)nf);
+    MO_CHECK_ARG(nf < ((int64_t)1 << 30) && nv < ((int64_t)1 << 31), "target mesh too large");
+    MO_CHECK_ARG(V && F && params4 && scratch && tree_out && status_out, "null pointer");
+    MO_CHECK_ARG((reinterpret_cast<uintptr_t>(tree_out) & 15) == 0, "tree_out must be 16-byte aligned");
+    const size_t need = plan_scratch(nullptr, nv, nf, MO_DF_LBVH).bytes;
+    if (scratch_bytes < need) {
+        set_error("tree build scratch too small: %zu < %zu", scratch_bytes, need);
+        return MO_ERR_SCRATCH;
+    }
+    cudaStream_t s = as_stream(stream);
+    BuildScratch S = plan_scratch(reinterpret_cast<char*>(scratch), nv, nf, MO_DF_LBVH);
+    float4* out = reinterpret_cast<float4*>(tree_out);
+    // the records are written straight into the output
+    S.tris = out;
+    S.tnodes = out + (size_t)TRI_F4 * nf;
+    k_normalize_copy<<<ceil_div(3 * nv, 256), 256, 0, s>>>(V, nv, params4, S.Vn); ::mo::note_launch();
+    cudaError_t e = issue_tree(S, F, nv, nf, reinterpret_cast<int*>(status_out), s);
+    if (e != cudaSuccess) return cuda_status(e, "mo_df_tree_build");
+    return MO_OK;
+}
 
 extern "C" int mo_bbox(const float* V, int64_t n, int32_t* bbox6, void* stream) {
     MO_CHECK_ARG(n >= 0, "negative vertex count");
@@ -943,22 +814,8 @@ extern "C" int mo_df_build_ex(const float* V, int64_t nv, const int32_t* F, int6
             k_df_brute<<<ceil_div(nvox, BF_THREADS), BF_THREADS, 0, s>>>(S.tris, (int)nf, N, band, band2, grid_out);
             ::mo::note_launch();
         } else {
-            k_morton<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.codes_a, S.ids_a, st); ::mo::note_launch();
-            e = radix_sort_pairs(S.codes_a, S.ids_a, S.codes_b, S.ids_b, (int)nf, 30, S.hist, s);
-            if (e != cudaSuccess) { fail(e, "radix_sort_pairs"); break; }
-            k_tri_records<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, S.ids_a, S.tris, S.boxes); ::mo::note_launch();
-            if (nf > 1) {
-                k_karras<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.codes_a, (int)nf, S.nodes, S.parent, S.flags, S.range);
-                ::mo::note_launch();
-                k_obb_exact<<<ceil_div(nf - 1, OBB_WARPS), OBB_WARPS * 32, 0, s>>>(S.range, (int)nf, S.tris, S.obb);
-                ::mo::note_launch();
-                k_obb_walk<<<ceil_div(nf, 256), 256, 0, s>>>(S.nodes, S.range, (int)nf, S.parent, S.flags, S.tris,
-                                                             S.obb, st);
-                ::mo::note_launch();
-                k_obb_nodes<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.nodes, S.range, (int)nf, S.tris, S.obb,
-                                                                  S.tnodes);
-                ::mo::note_launch();
-            }
+            e = issue_tree(S, F, nv, nf, st, s);
+            if (e != cudaSuccess) { fail(e, "LBVH build"); break; }
             launch_df_lbvh(packet, S.tnodes, S.tris, (int)nf, N, band, band2, grid_out, st, s);
         }
         e = cudaGetLastError();

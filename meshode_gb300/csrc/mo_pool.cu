@@ -48,6 +48,13 @@ struct Req {
     float* m = nullptr;
     float* v = nullptr;
     float* result = nullptr;  // [2][nv][3]: normalised, then denormalised
+    // on-demand distance field
+    bool lazy = false;
+    float* tree = nullptr;       // mo_df_tree_build output
+    float* lin = nullptr;        // N^3 voxel values
+    uint32_t* dfbits = nullptr;  // cell bits, then packet bits
+    MoPair* pair_dev = nullptr;  // one-row pair table for the seeding fill
+    int32_t* seedq = nullptr;    // seeding queues (nv cells, 8 nv packets) and their counters
     struct HostSlot* host = nullptr;
     int layout = MO_LAYOUT_CELL;
     int spt = MO_TILE_WARPS;
@@ -66,6 +73,7 @@ struct HostSlot {
     int32_t status[4];
     double loss;
     double pad;
+    MoPair pair;  // the request's pair row for its seeding fill
 };
 
 struct AdamTable {
@@ -105,6 +113,10 @@ struct MoPool {
     bool timing = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> group_events;
     std::vector<double> group_bytes;
+    int32_t* dfq = nullptr;        // on-demand cells queued by a step: (pair, cell)
+    int32_t* dfpq = nullptr;       // and their new voxel packets: (pair, packet)
+    int32_t* dfq_count = nullptr;  // two counters (cells, packets) per launch of a group
+    int dfq_cap = 0;
     MoPoolStats stats{};
 };
 
@@ -135,14 +147,19 @@ void free_state(Req* R, cudaStream_t s) {
     pfree(R->bbox, s); pfree(R->params, s); pfree(R->status, s); pfree(R->grid, s);
     pfree(R->csr, s); pfree(R->slice_ptr, s); pfree(R->sell, s); pfree(R->pos, s);
     pfree(R->rest, s); pfree(R->m, s); pfree(R->v, s);
+    pfree(R->tree, s); pfree(R->lin, s); pfree(R->dfbits, s); pfree(R->pair_dev, s); pfree(R->seedq, s);
 }
 
 // Peak device bytes one request holds from admission to retirement.
-size_t estimate(const MoRequest& q, int layout, int method) {
+size_t estimate(const MoRequest& q, int layout, int method, bool lazy) {
     const int64_t nv = q.nv, nh = 3 * q.nf, N = q.N;
     const size_t glin = (size_t)4 * N * N * N;
-    const size_t grid = layout == MO_LAYOUT_LINEAR ? glin : mo_grid_bytes((int)N, layout) + glin;
-    const size_t scratch = mo_df_build_scratch_bytes(q.ntv, q.ntf, (int)N, method);
+    size_t grid = layout == MO_LAYOUT_LINEAR ? glin : mo_grid_bytes((int)N, layout) + glin;
+    size_t scratch = mo_df_build_scratch_bytes(q.ntv, q.ntf, (int)N, method);
+    if (lazy) {
+        grid += mo_df_tree_bytes(q.ntf) + mo_df_lazy_bytes((int)N) + sizeof(MoPair) + 72 * (size_t)nv + 256;
+        scratch = mo_df_tree_scratch_bytes(q.ntv, q.ntf);
+    }
     const size_t meshes = (size_t)12 * (nv + q.nf + q.ntv + q.ntf);
     const size_t edges = mo_edge_csr_bytes(nv, q.nf, MO_EDGES_FACES);
     const size_t sell = (size_t)4 * (2 * nh + 32 * ((nv + 31) / 32) * 4);
@@ -186,6 +203,8 @@ void fail(MoPool* P, Req* R, const char* msg, cudaStream_t s) {
     P->completed.push_back(R->id);
 }
 
+void fill_pair(const MoPool* P, const Req* R, MoPair* p, int tile0);
+
 // Phase A on a build stream: input copies, target bbox and transform, DF
 // build (+ re-layout), source normalisation, CSR, sliced-ELL plan; then the
 // status words go to pinned host memory.
@@ -217,6 +236,21 @@ int phase_a(MoPool* P, Req* R) {
     if (!rc) rc = mo_norm_params(R->bbox, R->params, sv);
     if (rc) return rc;
     const int N = q.N;
+    if (R->lazy) {
+        // the tree now; the grid's cells when the steps reach them
+        const size_t sb = mo_df_tree_scratch_bytes(q.ntv, q.ntf);
+        void* scratch = nullptr;
+        PCHK(palloc(P, &scratch, sb, s));
+        PCHK(palloc(P, &R->tree, mo_df_tree_bytes(q.ntf), s));
+        rc = mo_df_tree_build(tarV, q.ntv, tarF, q.ntf, R->params, scratch, sb, R->tree, R->status, sv);
+        cudaFreeAsync(scratch, s);
+        if (rc) return rc;
+        PCHK(palloc(P, &R->lin, (size_t)4 * N * N * N, s));
+        PCHK(palloc(P, &R->grid, mo_grid_bytes(N, MO_LAYOUT_CELL), s));
+        const size_t lb = mo_df_lazy_bytes(N);
+        PCHK(palloc(P, &R->dfbits, lb, s));
+        PCHK(cudaMemsetAsync(R->dfbits, 0, lb, s));
+    } else {
     MoDfOptions opt;
     std::memset(&opt, 0, sizeof(opt));
     opt.method = R->method;
@@ -240,6 +274,7 @@ int phase_a(MoPool* P, Req* R) {
         rc = mo_grid_relayout(glin, N, R->layout, R->grid, sv);
         cudaFreeAsync(glin, s);
         if (rc) return rc;
+    }
     }
     pfree(R->tarV, s);
     pfree(R->tarF, s);
@@ -287,12 +322,27 @@ int phase_b(MoPool* P, Req* R) {
     if (rc) return rc;
     pfree(R->srcV, s);
     R->ntiles = (R->nslices + R->spt - 1) / R->spt;
+    if (R->lazy) {
+        // the cells of the starting positions, before the first step
+        fill_pair(P, R, &R->host->pair, 0);
+        PCHK(palloc(P, &R->pair_dev, sizeof(MoPair), s));
+        PCHK(cudaMemcpyAsync(R->pair_dev, &R->host->pair, sizeof(MoPair), cudaMemcpyHostToDevice, s));
+        PCHK(palloc(P, &R->seedq, 72 * (size_t)nv + 16, s));
+        int32_t* pq = R->seedq + 2 * nv;
+        int32_t* cnt = pq + 16 * nv;
+        PCHK(cudaMemsetAsync(cnt, 0, 8, s));
+        rc = mo_df_lazy_seed(R->pair_dev, 0, R->pos, nv, R->seedq, pq, cnt, (int)nv, sv);
+        if (!rc) rc = mo_df_lazy_fill(R->pair_dev, R->seedq, pq, cnt, (int)nv, sv);
+        if (rc) return rc;
+        pfree(R->seedq, s);
+        pfree(R->pair_dev, s);
+    }
     PCHK(cudaEventRecord(R->ev, s));
     R->phase = 2;
     return MO_OK;
 }
 
-void fill_pair(const Req* R, MoPair* p, int tile0) {
+void fill_pair(const MoPool* P, const Req* R, MoPair* p, int tile0) {
     std::memset(p, 0, sizeof(MoPair));
     p->grid = R->grid;
     p->slice_ptr = R->slice_ptr;
@@ -318,6 +368,21 @@ void fill_pair(const Req* R, MoPair* p, int tile0) {
     p->t_end = R->in.steps;
     p->tile0 = tile0;
     p->ntiles = R->ntiles;
+    if (R->lazy) {
+        const int N = R->in.N;
+        const int64_t cell_words = ((int64_t)(N - 1) * (N - 1) * (N - 1) + 31) / 32;
+        p->df_tree = R->tree;
+        p->df_lin = R->lin;
+        p->df_cells = R->dfbits;
+        p->df_packets = R->dfbits + cell_words;
+        p->df_status = R->status;
+        p->df_queue = P->dfq;
+        p->df_pqueue = P->dfpq;
+        p->df_queue_count = P->dfq_count;
+        p->df_ntri = (int32_t)R->in.ntf;
+        p->df_queue_cap = P->dfq_cap;
+        p->df_band = R->band;
+    }
 }
 
 // Pair table (every group: t0 moves) and tile table (only when the active
@@ -335,7 +400,7 @@ int upload(MoPool* P) {
     int tile0 = 0;
     for (int i = 0; i < n; ++i) {
         const Req* R = P->reqs[P->active[i]].get();
-        fill_pair(R, &ptab[i], tile0);
+        fill_pair(P, R, &ptab[i], tile0);
         tile0 += R->ntiles;
     }
     PCHK(cudaMemcpyAsync(P->pairs_dev, ptab, sizeof(MoPair) * (size_t)n, cudaMemcpyHostToDevice, P->step));
@@ -361,8 +426,13 @@ int upload(MoPool* P) {
 
 int launch_steps(MoPool* P) {
     void* sv = reinterpret_cast<void*>(P->step);
+    const bool lazy = P->cfg.df_mode == MO_DF_ON_DEMAND;
+    if (lazy) PCHK(cudaMemsetAsync(P->dfq_count, 0, 8 * (size_t)P->cfg.group_steps, P->step));
     for (int k = 0; k < P->cfg.group_steps; ++k) {
-        int rc = mo_fused_step(P->pairs_dev, P->tiles_dev, P->ntiles_dev, P->cfg.max_tiles, k, P->tile_loss, P->cfg.step_grid, sv);
+        int rc = mo_fused_step(P->pairs_dev, P->tiles_dev, P->ntiles_dev, P->cfg.max_tiles, k, P->tile_loss,
+                               P->cfg.step_grid, sv);
+        // the cells this step moved vertices into, before the next step reads them
+        if (!rc && lazy) rc = mo_df_lazy_fill(P->pairs_dev, P->dfq, P->dfpq, P->dfq_count + 2 * k, P->dfq_cap, sv);
         if (rc) return rc;
     }
     return MO_OK;
@@ -460,6 +530,8 @@ int run_group(MoPool* P) {
             PCHK(cudaMemcpyAsync(R->in.V_normalized_out, normed, 12 * nv, cudaMemcpyDeviceToDevice, P->step));
         PCHK(cudaMemcpyAsync(&R->host->loss, P->pair_loss + (int64_t)(k - 1) * n + i, 8, cudaMemcpyDeviceToHost,
                              P->step));
+        // DF status again: on-demand fills report traversal faults there
+        PCHK(cudaMemcpyAsync(R->host->status, R->status, 16, cudaMemcpyDeviceToHost, P->step));
         PCHK(cudaEventRecord(R->ev, P->step));
         free_state(R, P->step);
         R->phase = 4;
@@ -474,7 +546,7 @@ int progress(MoPool* P) {
     while (!P->queued.empty() && (int)P->building.size() < P->cfg.max_building &&
            (int)(P->active.size() + P->building.size() + P->retiring.size()) < P->cfg.max_pairs) {
         Req* R = P->reqs[P->queued.front()].get();
-        const size_t nb = estimate(R->in, R->layout, R->method);
+        const size_t nb = estimate(R->in, R->layout, R->method, R->lazy);
         const bool idle = P->active.empty() && P->building.empty() && P->retiring.empty();
         if (P->stats.bytes_in_use + nb > P->cfg.hbm_budget_bytes && !idle) break;
         P->queued.pop_front();
@@ -538,6 +610,12 @@ int progress(MoPool* P) {
             continue;
         }
         PCHK(q);
+        if (R->host->status[0]) {
+            char msg[128];
+            snprintf(msg, sizeof(msg), "distance-field fill failed (status %d)", R->host->status[0]);
+            fail(P, R, msg, P->step);
+            continue;
+        }
         R->state = MO_REQ_DONE;
         P->stats.bytes_in_use -= R->bytes;
         R->bytes = 0;
@@ -552,6 +630,7 @@ int progress(MoPool* P) {
     int t2 = 0;
     for (int64_t id : P->active) t2 += P->reqs[id]->ntiles;
     P->stats.active_tiles = t2;
+    P->stats.fill_launches_per_step = P->cfg.df_mode == MO_DF_ON_DEMAND ? 2 : 0;
     return MO_OK;
 }
 
@@ -626,6 +705,16 @@ int init_pool(MoPool* P) {
     PCHK(cudaMemset(P->ntiles_dev, 0, 4));
     PCHK(cudaMalloc(&P->tile_loss, sizeof(float) * (size_t)S * P->cfg.max_tiles * MO_TILE_WARPS));
     PCHK(cudaMalloc(&P->pair_loss, sizeof(double) * (size_t)S * P->cfg.max_pairs));
+    if (P->cfg.df_mode == MO_DF_ON_DEMAND) {
+        // a step queues at most one cell per vertex stepped
+        const int64_t cap = (int64_t)P->cfg.max_tiles * 32 * MO_TILE_WARPS;
+        MO_CHECK_ARG(cap < ((int64_t)1 << 28), "max_tiles too large for the on-demand cell queue");
+        P->dfq_cap = (int)cap;
+        PCHK(cudaMalloc(&P->dfq, 8 * (size_t)cap));
+        PCHK(cudaMalloc(&P->dfpq, 64 * (size_t)cap));
+        PCHK(cudaMalloc(&P->dfq_count, 8 * (size_t)S));
+        PCHK(cudaMemset(P->dfq_count, 0, 8 * (size_t)S));
+    }
     const size_t sbytes = sizeof(MoPair) * (size_t)P->cfg.max_pairs + sizeof(MoTile) * (size_t)P->cfg.max_tiles + 16;
     for (int i = 0; i < 2; ++i) {
         PCHK(cudaMallocHost(&P->staging[i], sbytes));
@@ -642,6 +731,7 @@ extern "C" int mo_pool_create(const MoPoolConfig* cfg, MoPool** out) {
     *out = nullptr;
     MO_CHECK_ARG(cfg->max_pairs > 0 && cfg->max_tiles > 0 && cfg->group_steps > 0, "bad pool sizes");
     MO_CHECK_ARG(mo_grid_bytes(64, cfg->layout) > 0, "unknown layout %d", cfg->layout);
+    MO_CHECK_ARG(cfg->df_mode == MO_DF_FULL || cfg->df_mode == MO_DF_ON_DEMAND, "unknown df_mode %d", cfg->df_mode);
     MoPool* P = new MoPool();
     P->cfg = *cfg;
     const int rc = init_pool(P);
@@ -665,6 +755,8 @@ extern "C" int mo_pool_submit(MoPool* P, const MoRequest* q, int64_t* id_out) {
     R->in = *q;
     R->layout = q->layout >= 0 ? q->layout : P->cfg.layout;
     MO_CHECK_ARG(mo_grid_bytes(q->N, R->layout) > 0, "unknown layout %d", R->layout);
+    R->lazy = P->cfg.df_mode == MO_DF_ON_DEMAND;
+    if (R->lazy) R->layout = MO_LAYOUT_CELL;  // the fills write cell records
     R->spt = (q->slices_per_tile > 0 && q->slices_per_tile <= MO_TILE_WARPS) ? q->slices_per_tile
                                                                             : P->cfg.slices_per_tile;
     MO_CHECK_ARG(q->df_method == MO_DF_AUTO || q->df_method == MO_DF_BRUTE || q->df_method == MO_DF_LBVH,
@@ -856,6 +948,9 @@ extern "C" int mo_pool_destroy(MoPool* P) {
     for (auto& a : P->adam_tabs) cudaFree(a.dev);
     if (P->graph) cudaGraphExecDestroy(P->graph);
     cudaFree(P->pairs_dev);
+    cudaFree(P->dfq);
+    cudaFree(P->dfpq);
+    cudaFree(P->dfq_count);
     cudaFree(P->tiles_dev);
     cudaFree(P->ntiles_dev);
     cudaFree(P->tile_loss);

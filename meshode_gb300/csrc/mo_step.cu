@@ -6,7 +6,7 @@
 // RigidLossFunction (src/python/layers/rigid_loss_layer.py:7-27) or
 // GraphLossFunction (src/python/layers/graph_loss_layer.py:9-43) and
 // torch.optim.Adam.
-#include "mo_df_eval.cuh"
+#include "mo_lazydf.cuh"
 
 namespace mo {
 
@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(256) k_adam(float* __restrict__ P, const float
 constexpr int STEP_THREADS = 256;  // 8 warps = up to 8 slices of 32 vertices
 constexpr int TILE_WARPS = STEP_THREADS / 32;
 static_assert(TILE_WARPS == MO_TILE_WARPS, "tile warps");
-constexpr int REC_UNROLL = 2;      // record rows fetched ahead of their neighbour gathers
+constexpr int REC_UNROLL = 3;      // record rows whose neighbours are gathered together
 
 template <int LAYOUT>
 __device__ __forceinline__ DFJet df_eval_layout(const float* grid, int N, float Nf, float Cf, float x, float y,
@@ -72,11 +72,18 @@ __global__ void __launch_bounds__(STEP_THREADS, 4) k_fused_step(const MoPair* __
         const float4 r0 = valid ? __ldg(R + i) : zero;
         float* __restrict__ Mm = P.adam_m + 3 * (int64_t)i;
         float* __restrict__ Vv = P.adam_v + 3 * (int64_t)i;
-        float m0 = 0.f, m1 = 0.f, m2 = 0.f, v0 = 0.f, v1 = 0.f, v2 = 0.f;
-        if (valid) {
-            m0 = Mm[0]; m1 = Mm[1]; m2 = Mm[2];
-            v0 = Vv[0]; v1 = Vv[1]; v2 = Vv[2];
+        if (valid) {  // the moments are read after the edge loop
+            asm volatile("prefetch.global.L1 [%0];" :: "l"(Mm));
+            asm volatile("prefetch.global.L1 [%0];" :: "l"(Vv));
         }
+        // The first record rows are requested before the distance-field cell
+        // so that both gathers are in flight together.
+        const int rb = P.slice_ptr[slice];
+        const int rows = (P.slice_ptr[slice + 1] - rb) >> 5;
+        const int* __restrict__ rec = P.sell + rb + lane;
+        int c[REC_UNROLL];
+#pragma unroll
+        for (int u = 0; u < REC_UNROLL; ++u) c[u] = (u < rows) ? __ldg(rec + u * 32) : -1;
         const int N = P.N;
         const float Nf = (float)N, Cf = (float)((double)(N - 1) - 1e-3);
         const DFJet j = (P.layout == MO_LAYOUT_CELL)
@@ -94,14 +101,10 @@ __global__ void __launch_bounds__(STEP_THREADS, 4) k_fused_step(const MoPair* __
         }
         // Edge residuals over this vertex's sliced-ELL column, in the order
         // of the reference's serial scatter.  Rest offset = rest[v1] - rest[v0].
+        // The next rows' records are requested while this row's neighbours
+        // are gathered.
         float grx = 0.f, gry = 0.f, grz = 0.f, esq = 0.f;
-        const int rb = P.slice_ptr[slice];
-        const int rows = (P.slice_ptr[slice + 1] - rb) >> 5;
-        const int* __restrict__ rec = P.sell + rb + lane;
         for (int row = 0; row < rows; row += REC_UNROLL) {
-            int c[REC_UNROLL];
-#pragma unroll
-            for (int u = 0; u < REC_UNROLL; ++u) c[u] = (row + u < rows) ? __ldg(rec + (row + u) * 32) : -1;
             float4 q[REC_UNROLL], sr[REC_UNROLL];
 #pragma unroll
             for (int u = 0; u < REC_UNROLL; ++u) {
@@ -114,23 +117,28 @@ __global__ void __launch_bounds__(STEP_THREADS, 4) k_fused_step(const MoPair* __
                     sr[u] = zero;
                 }
             }
+            int cn[REC_UNROLL];
+#pragma unroll
+            for (int u = 0; u < REC_UNROLL; ++u)
+                cn[u] = (row + REC_UNROLL + u < rows) ? __ldg(rec + (row + REC_UNROLL + u) * 32) : -1;
+            // As v0 of a half-edge the vertex takes g -= r with r = (v1 - v0) - off;
+            // as v1 it takes g += (v0 - v1) - (-off), which is the same
+            // rounding of the same r with its sign flipped, so both roles
+            // subtract r = (q - p) - (rest[q] - rest[p]); only v0 adds the
+            // edge's energy.  Padding (-1) follows the last real record.
 #pragma unroll
             for (int u = 0; u < REC_UNROLL; ++u) {
-                if (c[u] == -1) break;  // padding follows the last real record
-                if (c[u] >= 0) {  // vertex is v0 of the half-edge: g -= v1 - v0 - off
-                    const float rx = SUB(SUB(q[u].x, p.x), SUB(sr[u].x, r0.x));
-                    const float ry = SUB(SUB(q[u].y, p.y), SUB(sr[u].y, r0.y));
-                    const float rz = SUB(SUB(q[u].z, p.z), SUB(sr[u].z, r0.z));
+                const float rx = SUB(SUB(q[u].x, p.x), SUB(sr[u].x, r0.x));
+                const float ry = SUB(SUB(q[u].y, p.y), SUB(sr[u].y, r0.y));
+                const float rz = SUB(SUB(q[u].z, p.z), SUB(sr[u].z, r0.z));
+                if (c[u] != -1) {
                     grx = SUB(grx, rx); gry = SUB(gry, ry); grz = SUB(grz, rz);
-                    esq += rx * rx + ry * ry + rz * rz;
-                } else {          // vertex is v1: g += v1 - v0 - off
-                    const float rx = SUB(SUB(p.x, q[u].x), SUB(r0.x, sr[u].x));
-                    const float ry = SUB(SUB(p.y, q[u].y), SUB(r0.y, sr[u].y));
-                    const float rz = SUB(SUB(p.z, q[u].z), SUB(r0.z, sr[u].z));
-                    grx = ADD(grx, rx); gry = ADD(gry, ry); grz = ADD(grz, rz);
                 }
+                if (c[u] >= 0) esq += rx * rx + ry * ry + rz * rz;
             }
             if (c[REC_UNROLL - 1] == -1) break;
+#pragma unroll
+            for (int u = 0; u < REC_UNROLL; ++u) c[u] = cn[u];
         }
         // grad_h * (gD + gR * w)  (graph_loss_layer.py:42, rigid_loss_layer.py:27)
         const float we = P.w_edge, gh = P.grad_scale;
@@ -145,6 +153,8 @@ __global__ void __launch_bounds__(STEP_THREADS, 4) k_fused_step(const MoPair* __
                 P.grad_dbg[3 * (int64_t)i + 2] = gz;
             }
             const float2 ab = __ldg(reinterpret_cast<const float2*>(P.adam_tab) + (t - 1));
+            float m0 = Mm[0], m1 = Mm[1], m2 = Mm[2];
+            float v0 = Vv[0], v1 = Vv[1], v2 = Vv[2];
             float px = p.x, py = p.y, pz = p.z;
             adam_elem(px, gx, m0, v0, P.one_minus_b1, P.b2, P.one_minus_b2, P.eps, ab.x, ab.y);
             adam_elem(py, gy, m1, v1, P.one_minus_b1, P.b2, P.one_minus_b2, P.eps, ab.x, ab.y);
@@ -152,6 +162,12 @@ __global__ void __launch_bounds__(STEP_THREADS, 4) k_fused_step(const MoPair* __
             Mm[0] = m0; Mm[1] = m1; Mm[2] = m2;
             Vv[0] = v0; Vv[1] = v1; Vv[2] = v2;
             Vout[i] = make_float4(px, py, pz, 0.f);
+            if (P.df_cells != nullptr && t < P.t_end) {  // on-demand grid: the next step's cell
+                int cn = lazy_cell_of(N, px, py, pz);
+                if (cn == lazy_cell_of(N, p.x, p.y, p.z)) cn = -1;  // read by this step: written
+                lazy_queue_cell(P, T.pair, cn, P.df_queue, P.df_pqueue, P.df_queue_count + 2 * k,
+                                P.df_queue_cap);
+            }
             part = 0.5f * dsq + we * (0.5f * esq);
         }
         for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);

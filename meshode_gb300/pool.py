@@ -20,7 +20,8 @@ from ._lib import check
 class NativePool:
     def __init__(self, device=None, hbm_budget_bytes=None, max_pairs=512, max_tiles=None, group_steps=25,
                  layout=L.MO_LAYOUT_CELL, use_graph=True, max_building=16, results_to_host=True, build_streams=6,
-                 slices_per_tile=L.MO_TILE_WARPS, autotuner=None, df_band=-1.0, step_grid=0):
+                 slices_per_tile=L.MO_TILE_WARPS, autotuner=None, df_band=-1.0, step_grid=0,
+                 df_mode=L.MO_DF_FULL):
         L.require_cuda()
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
         self.lib = L.lib()
@@ -28,7 +29,11 @@ class NativePool:
             hbm_budget_bytes=int(hbm_budget_bytes or 0), max_pairs=int(max_pairs),
             max_tiles=int(max_tiles if max_tiles is not None else 1 << 17), group_steps=int(group_steps),
             use_graph=1 if use_graph else 0, max_building=int(max_building), build_streams=int(build_streams),
-            layout=int(layout), slices_per_tile=int(slices_per_tile), step_grid=int(step_grid))
+            layout=int(layout), slices_per_tile=int(slices_per_tile), step_grid=int(step_grid),
+            df_mode=int(df_mode))
+        # MO_DF_ON_DEMAND: grids are filled cell by cell as the vertices reach
+        # them (cell layout); MO_DF_FULL: every grid is built at admission
+        self.df_mode = int(df_mode)
         self.S = int(group_steps)
         self.layout = int(layout)
         self.autotuner = autotuner
@@ -65,8 +70,10 @@ class NativePool:
 
     @property
     def launches(self):
-        """mo_fused_step launches issued (a graph replay counts its S launches)."""
-        return int(self.stats().fused_launches)
+        """Kernels of the step groups issued: mo_fused_step launches (a graph
+        replay counts its S launches) and the on-demand fills after them."""
+        st = self.stats()
+        return int(st.fused_launches) * (1 + int(st.fill_launches_per_step))
 
     @property
     def peak_in_use(self):

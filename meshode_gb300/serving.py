@@ -62,13 +62,17 @@ class Request:
         return None if self.t_done is None else self.t_done - self.t_arrive
 
 
-def estimate_bytes(nv, nf_src, nv_tar, nf_tar, N, layout=L.MO_LAYOUT_CELL):
+def estimate_bytes(nv, nf_src, nv_tar, nf_tar, N, layout=L.MO_LAYOUT_CELL, df_mode=L.MO_DF_FULL):
     """Peak device bytes one request holds from admission to retirement
-    (the grid counted in the largest layout)."""
+    (the grid counted in the largest layout); df_mode MO_DF_ON_DEMAND adds
+    the native pool's traversal tree, cell bits and seeding queue."""
     lib = L.lib()
     nh = 3 * nf_src
     grid = max(lib.mo_grid_bytes(N, lay) for lay in (L.MO_LAYOUT_CELL, L.MO_LAYOUT_BRICK4, layout)) + 4 * N ** 3
     scratch = lib.mo_df_build_scratch_bytes(nv_tar, nf_tar, N, L.MO_DF_AUTO)
+    if df_mode == L.MO_DF_ON_DEMAND:
+        grid += lib.mo_df_tree_bytes(nf_tar) + lib.mo_df_lazy_bytes(N) + ctypes.sizeof(L.MoPair) + 72 * nv + 256
+        scratch = lib.mo_df_tree_scratch_bytes(nv_tar, nf_tar)
     meshes = 12 * (nv + nf_src + nv_tar + nf_tar)
     edges = lib.mo_edge_csr_bytes(nv, nf_src, L.MO_EDGES_FACES)
     sell = 4 * (2 * nh + 32 * ((nv + 31) // 32) * 4)

@@ -12,6 +12,7 @@
 import pytest
 import torch
 
+from meshode_gb300 import _lib as L
 from meshode_gb300 import fused, meshgen, pool, serving
 from meshode_gb300 import pyDeform as PD
 
@@ -112,12 +113,15 @@ def test_pool_bad_request_is_isolated(cuda):
 def test_pool_admission_respects_budget(cuda):
     specs, meshes = _stream(n=6, seed=9)
     reqs = serving.requests_from_meshes(meshes, specs, device=None, pin=True)
-    one = max(serving.estimate_bytes(r.srcV.shape[0], r.srcF.shape[0], r.tarV.shape[0], r.tarF.shape[0], r.N)
-              for r in reqs)
-    P = pool.NativePool(group_steps=8, hbm_budget_bytes=int(one * 1.5))
-    P.run(reqs)
-    assert all(r.out is not None for r in reqs)
-    assert 0 < P.peak_in_use <= int(one * 1.5)
+    for mode in (L.MO_DF_FULL, L.MO_DF_ON_DEMAND):
+        one = max(serving.estimate_bytes(r.srcV.shape[0], r.srcF.shape[0], r.tarV.shape[0], r.tarF.shape[0], r.N,
+                                         df_mode=mode) for r in reqs)
+        P = pool.NativePool(group_steps=8, hbm_budget_bytes=int(one * 1.5), df_mode=mode)
+        part = _fresh(reqs)
+        P.run(part)
+        assert all(r.out is not None for r in part)
+        assert 0 < P.peak_in_use <= int(one * 1.5)
+        P.close()
 
 
 def test_pool_steady_state(cuda):
