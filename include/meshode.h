@@ -294,6 +294,10 @@ typedef struct MoTile {
 #define MO_TILE_WARPS 8
 int mo_fused_step(const MoPair* pairs, const MoTile* tiles, const int32_t* ntiles, int max_tiles,
                   int launch_index, float* tile_loss, int grid_ctas, void* stream);
+/* mo_fused_step for pairs with on-demand grids (df_cells set): also queues
+ * the cells the step moves vertices into (see MoPair). */
+int mo_fused_step_on_demand(const MoPair* pairs, const MoTile* tiles, const int32_t* ntiles, int max_tiles,
+                            int launch_index, float* tile_loss, int grid_ctas, void* stream);
 /* pair_loss[k*npairs + p] (double) = sum, in a fixed order, of the tile
  * partials of pair p (its MoPair tile0/ntiles range) for launches
  * k = 0..nlaunch-1: the layer loss 0.5*sum d^2 + w_edge*0.5*sum |r|^2 at the
@@ -306,14 +310,15 @@ int mo_pair_loss(const MoPair* pairs, int npairs, int max_tiles, int nlaunch, co
  * and their packets, as a step does: cells into queue (cap entries),
  * packets into pqueue (8 * cap entries), counts[0] / counts[1] counting
  * them.  mo_df_lazy_fill computes the queued packets, then writes the
- * queued cells.  Both read the pair table from device memory.  Grids up to
+ * queued cells, and adds the two counts to totals[0..1] (device int64,
+ * optional).  Both read the pair table from device memory.  Grids up to
  * MO_DF_LAZY_MAX_N per axis (df_status bit 16 above it). */
 #define MO_DF_LAZY_MAX_N 1024
 size_t mo_df_lazy_bytes(int N);
 int mo_df_lazy_seed(const MoPair* pairs, int pair, const float* pos4, int64_t nv, int32_t* queue,
                     int32_t* pqueue, int32_t* counts, int cap, void* stream);
 int mo_df_lazy_fill(const MoPair* pairs, const int32_t* queue, const int32_t* pqueue, const int32_t* counts,
-                    int cap, void* stream);
+                    int cap, int64_t* totals, void* stream);
 
 /* ------------------------------------------------------------------------
  * Serving pool: admit / step / retire deformation requests.  A request is one
@@ -427,6 +432,10 @@ int mo_pool_run_groups(MoPool* pool, int groups);
  * algorithmic bytes (104 per vertex + 44 per half-edge per pair-step). */
 int mo_pool_group_time(MoPool* pool, double* ms_out, double* bytes_out);
 int mo_pool_stats(MoPool* pool, MoPoolStats* out);
+/* On-demand mode: cells written and voxel packets computed so far, over all
+ * requests (out2[0], out2[1]); zeros for full grids.  Synchronises the
+ * pool's streams. */
+int mo_pool_fill_totals(MoPool* pool, int64_t* out2);
 /* Return freed device memory the pool keeps for reuse to the device, down to
  * keep_bytes (synchronises the pool's streams). */
 int mo_pool_trim(MoPool* pool, uint64_t keep_bytes);

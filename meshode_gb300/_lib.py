@@ -95,7 +95,7 @@ _SIGS = {
     "mo_df_tree_build": (_I, [_P, _I64, _P, _I64, _P, _P, _SZ, _P, _P, _P]),
     "mo_df_lazy_bytes": (_SZ, [_I]),
     "mo_df_lazy_seed": (_I, [_P, _I, _P, _I64, _P, _P, _P, _I, _P]),
-    "mo_df_lazy_fill": (_I, [_P, _P, _P, _P, _I, _P]),
+    "mo_df_lazy_fill": (_I, [_P, _P, _P, _P, _I, _P, _P]),
     "mo_lbvh_build": (_I, [_P, _I64, _P, _I64, _P, _P, _SZ, _P, _P, _P, _P, _P, _P]),
     "mo_grid_bytes": (_SZ, [_I, _I]),
     "mo_grid_relayout": (_I, [_P, _I, _I, _P, _P]),
@@ -112,6 +112,7 @@ _SIGS = {
     "mo_sell_fill": (_I, [_P, _I64, _I64, _P, _P, _P]),
     "mo_adam_step": (_I, [_P, _P, _P, _P, _I64, _F, _F, _F, _F, _F, _F, _P]),
     "mo_fused_step": (_I, [_P, _P, _P, _I, _I, _P, _I, _P]),
+    "mo_fused_step_on_demand": (_I, [_P, _P, _P, _I, _I, _P, _I, _P]),
     "mo_pair_loss": (_I, [_P, _I, _I, _I, _P, _P, _P]),
     "mo_abi_sizes": (_I, [ctypes.POINTER(_SZ), ctypes.POINTER(_SZ)]),
     "mo_mlp_in": (_I, [_P, _I64, _P, _P, _I, _P, _P, _P]),
@@ -145,6 +146,7 @@ _SIGS = {
     "mo_pool_run_groups": (_I, [_P, _I]),
     "mo_pool_group_time": (_I, [_P, _P, _P]),
     "mo_pool_stats": (_I, [_P, _P]),
+    "mo_pool_fill_totals": (_I, [_P, _P]),
     "mo_pool_trim": (_I, [_P, ctypes.c_uint64]),
     "mo_pool_step_stream": (_I, [_P, _P]),
 }

@@ -72,8 +72,13 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) k_lazy_packets(const MoPair* 
 // voxel values into the cell-layout grid.
 __global__ void __launch_bounds__(256) k_lazy_cells(const MoPair* __restrict__ pairs,
                                                     const int32_t* __restrict__ queue,
-                                                    const int32_t* __restrict__ counts, int cap) {
+                                                    const int32_t* __restrict__ counts, int cap,
+                                                    unsigned long long* __restrict__ totals) {
     const int64_t n = min(counts[0], cap);
+    if (totals && blockIdx.x == 0 && threadIdx.x == 0) {
+        atomicAdd(totals, (unsigned long long)n);
+        atomicAdd(totals + 1, (unsigned long long)min((int64_t)counts[1], 8 * (int64_t)cap));
+    }
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
         const int pair = queue[2 * e], c = queue[2 * e + 1];
         const MoPair& P = pairs[pair];
@@ -111,7 +116,7 @@ extern "C" int mo_df_lazy_seed(const MoPair* pairs, int pair, const float* pos4,
 }
 
 extern "C" int mo_df_lazy_fill(const MoPair* pairs, const int32_t* queue, const int32_t* pqueue,
-                               const int32_t* counts, int cap, void* stream) {
+                               const int32_t* counts, int cap, int64_t* totals, void* stream) {
     MO_CHECK_ARG(cap >= 0 && cap < (1 << 28), "bad queue capacity");
     MO_CHECK_ARG(pairs && queue && pqueue && counts, "null pointer");
     cudaStream_t s = as_stream(stream);
@@ -120,7 +125,7 @@ extern "C" int mo_df_lazy_fill(const MoPair* pairs, const int32_t* queue, const 
     const int sms = device_sm_count();
     k_lazy_packets<<<4 * sms, TRAV_WARPS * 32, 0, s>>>(pairs, pqueue, counts, cap);
     ::mo::note_launch();
-    k_lazy_cells<<<sms, 256, 0, s>>>(pairs, queue, counts, cap);
+    k_lazy_cells<<<sms, 256, 0, s>>>(pairs, queue, counts, cap, reinterpret_cast<unsigned long long*>(totals));
     ::mo::note_launch();
     MO_LAUNCH_CHECK("k_lazy_cells");
     return MO_OK;

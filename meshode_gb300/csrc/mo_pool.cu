@@ -117,6 +117,7 @@ struct MoPool {
     int32_t* dfpq = nullptr;       // and their new voxel packets: (pair, packet)
     int32_t* dfq_count = nullptr;  // two counters (cells, packets) per launch of a group
     int dfq_cap = 0;
+    int64_t* fill_totals = nullptr;  // device: cells written, packets computed
     MoPoolStats stats{};
 };
 
@@ -332,7 +333,7 @@ int phase_b(MoPool* P, Req* R) {
         int32_t* cnt = pq + 16 * nv;
         PCHK(cudaMemsetAsync(cnt, 0, 8, s));
         rc = mo_df_lazy_seed(R->pair_dev, 0, R->pos, nv, R->seedq, pq, cnt, (int)nv, sv);
-        if (!rc) rc = mo_df_lazy_fill(R->pair_dev, R->seedq, pq, cnt, (int)nv, sv);
+        if (!rc) rc = mo_df_lazy_fill(R->pair_dev, R->seedq, pq, cnt, (int)nv, P->fill_totals, sv);
         if (rc) return rc;
         pfree(R->seedq, s);
         pfree(R->pair_dev, s);
@@ -429,10 +430,12 @@ int launch_steps(MoPool* P) {
     const bool lazy = P->cfg.df_mode == MO_DF_ON_DEMAND;
     if (lazy) PCHK(cudaMemsetAsync(P->dfq_count, 0, 8 * (size_t)P->cfg.group_steps, P->step));
     for (int k = 0; k < P->cfg.group_steps; ++k) {
-        int rc = mo_fused_step(P->pairs_dev, P->tiles_dev, P->ntiles_dev, P->cfg.max_tiles, k, P->tile_loss,
-                               P->cfg.step_grid, sv);
+        int rc = (lazy ? mo_fused_step_on_demand : mo_fused_step)(P->pairs_dev, P->tiles_dev, P->ntiles_dev,
+                                                                  P->cfg.max_tiles, k, P->tile_loss,
+                                                                  P->cfg.step_grid, sv);
         // the cells this step moved vertices into, before the next step reads them
-        if (!rc && lazy) rc = mo_df_lazy_fill(P->pairs_dev, P->dfq, P->dfpq, P->dfq_count + 2 * k, P->dfq_cap, sv);
+        if (!rc && lazy)
+            rc = mo_df_lazy_fill(P->pairs_dev, P->dfq, P->dfpq, P->dfq_count + 2 * k, P->dfq_cap, P->fill_totals, sv);
         if (rc) return rc;
     }
     return MO_OK;
@@ -442,8 +445,10 @@ int launch_steps(MoPool* P) {
 // loads the kernel outside the capture.
 int capture(MoPool* P) {
     PCHK(cudaMemsetAsync(P->ntiles_dev, 0, 4, P->step));
-    int rc = mo_fused_step(P->pairs_dev, P->tiles_dev, P->ntiles_dev, P->cfg.max_tiles, 0, P->tile_loss, 0,
-                           reinterpret_cast<void*>(P->step));
+    const bool lazy = P->cfg.df_mode == MO_DF_ON_DEMAND;
+    int rc = (lazy ? mo_fused_step_on_demand : mo_fused_step)(P->pairs_dev, P->tiles_dev, P->ntiles_dev,
+                                                              P->cfg.max_tiles, 0, P->tile_loss, 0,
+                                                              reinterpret_cast<void*>(P->step));
     if (rc) return rc;
     PCHK(cudaStreamSynchronize(P->step));
     P->tiles_key.clear();  // the tile count was zeroed: re-send the table
@@ -714,6 +719,8 @@ int init_pool(MoPool* P) {
         PCHK(cudaMalloc(&P->dfpq, 64 * (size_t)cap));
         PCHK(cudaMalloc(&P->dfq_count, 8 * (size_t)S));
         PCHK(cudaMemset(P->dfq_count, 0, 8 * (size_t)S));
+        PCHK(cudaMalloc(&P->fill_totals, 16));
+        PCHK(cudaMemset(P->fill_totals, 0, 16));
     }
     const size_t sbytes = sizeof(MoPair) * (size_t)P->cfg.max_pairs + sizeof(MoTile) * (size_t)P->cfg.max_tiles + 16;
     for (int i = 0; i < 2; ++i) {
@@ -921,6 +928,16 @@ extern "C" int mo_pool_stats(MoPool* P, MoPoolStats* out) {
     return MO_OK;
 }
 
+extern "C" int mo_pool_fill_totals(MoPool* P, int64_t* out2) {
+    MO_CHECK_ARG(P && out2, "null pointer");
+    out2[0] = out2[1] = 0;
+    if (!P->fill_totals) return MO_OK;
+    PCHK(cudaStreamSynchronize(P->step));
+    for (cudaStream_t s : P->builds) PCHK(cudaStreamSynchronize(s));
+    PCHK(cudaMemcpy(out2, P->fill_totals, 16, cudaMemcpyDeviceToHost));
+    return MO_OK;
+}
+
 extern "C" int mo_pool_trim(MoPool* P, uint64_t keep_bytes) {
     MO_CHECK_ARG(P, "null pool");
     PCHK(cudaStreamSynchronize(P->step));
@@ -950,6 +967,7 @@ extern "C" int mo_pool_destroy(MoPool* P) {
     cudaFree(P->pairs_dev);
     cudaFree(P->dfq);
     cudaFree(P->dfpq);
+    cudaFree(P->fill_totals);
     cudaFree(P->dfq_count);
     cudaFree(P->tiles_dev);
     cudaFree(P->ntiles_dev);

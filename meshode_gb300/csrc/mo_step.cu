@@ -44,7 +44,11 @@ __device__ __forceinline__ DFJet df_eval_layout(const float* grid, int N, float 
 }
 
 // Every warp owns one 32-vertex slice of a tile and never waits for the
-// other warps of its block.
+// other warps of its block.  ON_DEMAND: the pairs' grids are filled on
+// demand, and a vertex moving into a cell not yet filled queues it (a
+// separate instantiation: the queueing code slows the plain kernel down even
+// when it is skipped).
+template <bool ON_DEMAND>
 __global__ void __launch_bounds__(STEP_THREADS, 4) k_fused_step(const MoPair* __restrict__ pairs,
                                                              const MoTile* __restrict__ tiles,
                                                              const int* __restrict__ ntiles_p, int max_tiles,
@@ -162,7 +166,7 @@ __global__ void __launch_bounds__(STEP_THREADS, 4) k_fused_step(const MoPair* __
             Mm[0] = m0; Mm[1] = m1; Mm[2] = m2;
             Vv[0] = v0; Vv[1] = v1; Vv[2] = v2;
             Vout[i] = make_float4(px, py, pz, 0.f);
-            if (P.df_cells != nullptr && t < P.t_end) {  // on-demand grid: the next step's cell
+            if (ON_DEMAND && P.df_cells != nullptr && t < P.t_end) {  // the next step's cell
                 int cn = lazy_cell_of(N, px, py, pz);
                 if (cn == lazy_cell_of(N, p.x, p.y, p.z)) cn = -1;  // read by this step: written
                 lazy_queue_cell(P, T.pair, cn, P.df_queue, P.df_pqueue, P.df_queue_count + 2 * k,
@@ -213,7 +217,8 @@ static int g_step_ctas = 0;
 static int step_ctas() {
     if (g_step_ctas == 0) {
         int per_sm = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_step, STEP_THREADS, 0) != cudaSuccess ||
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_step<false>, STEP_THREADS, 0) !=
+                cudaSuccess ||
             per_sm <= 0)
             per_sm = 4;
         g_step_ctas = per_sm * device_sm_count();
@@ -236,17 +241,33 @@ extern "C" int mo_adam_step(float* P, const float* G, float* M, float* Vsq, int6
     return MO_OK;
 }
 
-extern "C" int mo_fused_step(const MoPair* pairs, const MoTile* tiles, const int32_t* ntiles, int max_tiles,
-                             int launch_index, float* tile_loss, int grid_ctas, void* stream) {
+static int launch_fused_step(bool on_demand, const MoPair* pairs, const MoTile* tiles, const int32_t* ntiles,
+                             int max_tiles, int launch_index, float* tile_loss, int grid_ctas, void* stream) {
     MO_CHECK_ARG(pairs && tiles && ntiles && tile_loss, "null pointer");
     MO_CHECK_ARG(max_tiles >= 0 && launch_index >= 0, "negative size");
     if (max_tiles == 0) return MO_OK;
     int ctas = grid_ctas > 0 ? grid_ctas : step_ctas();
     if (ctas > max_tiles) ctas = max_tiles;
-    k_fused_step<<<ctas, STEP_THREADS, 0, as_stream(stream)>>>(pairs, tiles, ntiles, max_tiles, launch_index,
-                                                              tile_loss); ::mo::note_launch();
+    if (on_demand)
+        k_fused_step<true><<<ctas, STEP_THREADS, 0, as_stream(stream)>>>(pairs, tiles, ntiles, max_tiles,
+                                                                         launch_index, tile_loss);
+    else
+        k_fused_step<false><<<ctas, STEP_THREADS, 0, as_stream(stream)>>>(pairs, tiles, ntiles, max_tiles,
+                                                                          launch_index, tile_loss);
+    ::mo::note_launch();
     MO_LAUNCH_CHECK("k_fused_step");
     return MO_OK;
+}
+
+extern "C" int mo_fused_step(const MoPair* pairs, const MoTile* tiles, const int32_t* ntiles, int max_tiles,
+                             int launch_index, float* tile_loss, int grid_ctas, void* stream) {
+    return launch_fused_step(false, pairs, tiles, ntiles, max_tiles, launch_index, tile_loss, grid_ctas, stream);
+}
+
+extern "C" int mo_fused_step_on_demand(const MoPair* pairs, const MoTile* tiles, const int32_t* ntiles,
+                                       int max_tiles, int launch_index, float* tile_loss, int grid_ctas,
+                                       void* stream) {
+    return launch_fused_step(true, pairs, tiles, ntiles, max_tiles, launch_index, tile_loss, grid_ctas, stream);
 }
 
 extern "C" int mo_pair_loss(const MoPair* pairs, int npairs, int max_tiles, int nlaunch, const float* tile_loss,

@@ -75,6 +75,12 @@ class NativePool:
         st = self.stats()
         return int(st.fused_launches) * (1 + int(st.fill_launches_per_step))
 
+    def fill_totals(self):
+        """On-demand grids: (cells written, voxel packets computed) so far."""
+        out = (ctypes.c_int64 * 2)()
+        check(self.lib.mo_pool_fill_totals(self._h, out), "mo_pool_fill_totals")
+        return int(out[0]), int(out[1])
+
     @property
     def peak_in_use(self):
         return int(self.stats().peak_bytes)

@@ -87,8 +87,10 @@ def test_lazy_fill_matches_full_build(cuda, N, band_kind, seed):
     pqueue = torch.empty(16 * n, dtype=torch.int32, device=cuda)
     count = torch.zeros(2, dtype=torch.int32, device=cuda)
     call("mo_df_lazy_seed", ptr(pair_dev), 0, ptr(Pd), n, ptr(queue), ptr(pqueue), ptr(count), n, s)
-    call("mo_df_lazy_fill", ptr(pair_dev), ptr(queue), ptr(pqueue), ptr(count), n, s)
+    totals = torch.zeros(2, dtype=torch.int64, device=cuda)
+    call("mo_df_lazy_fill", ptr(pair_dev), ptr(queue), ptr(pqueue), ptr(count), n, ptr(totals), s)
     torch.cuda.synchronize()
+    assert totals.tolist() == count.tolist()
     assert status.tolist() == [0, 0, 0, 0]
     want = _cells_of(P, N)
     got = np.sort(queue[: 2 * int(count[0].item())].view(-1, 2)[:, 1].cpu().numpy())
@@ -112,7 +114,7 @@ def test_lazy_fill_matches_full_build(cuda, N, band_kind, seed):
     # a second fill of the same cells finds them queued and changes nothing
     count.zero_()
     call("mo_df_lazy_seed", ptr(pair_dev), 0, ptr(Pd), n, ptr(queue), ptr(pqueue), ptr(count), n, s)
-    call("mo_df_lazy_fill", ptr(pair_dev), ptr(queue), ptr(pqueue), ptr(count), n, s)
+    call("mo_df_lazy_fill", ptr(pair_dev), ptr(queue), ptr(pqueue), ptr(count), n, None, s)
     assert count.tolist() == [0, 0]
 
 
@@ -121,7 +123,7 @@ def test_lazy_arguments_are_checked(cuda):
     assert lib.mo_df_lazy_bytes(1) == 0 and lib.mo_df_lazy_bytes(L.MO_DF_LAZY_MAX_N + 1) == 0
     assert lib.mo_df_lazy_bytes(64) == 4 * ((63 ** 3 + 31) // 32 + (16 * 16 * 32 + 31) // 32)
     assert lib.mo_df_tree_bytes(0) == 0 and lib.mo_df_tree_bytes(10) == 16 * (5 * 10 + 8 * 9)
-    assert lib.mo_df_lazy_fill(None, None, None, None, 0, None) == L.MO_ERR_INVALID
+    assert lib.mo_df_lazy_fill(None, None, None, None, 0, None, None) == L.MO_ERR_INVALID
     assert lib.mo_df_tree_build(None, 0, None, 0, None, None, 0, None, None, None) == L.MO_ERR_INVALID
 
 
@@ -144,6 +146,8 @@ def test_on_demand_pool_matches_full_grids(cuda):
     Pl.run(lazy)
     st = Pl.stats()
     assert st.fill_launches_per_step == 2 and st.failed == 0
+    cells, packets = Pl.fill_totals()
+    assert 0 < packets and 0 < cells
     Pl.close()
     for a, b in zip(full, lazy):
         assert a.error is None and b.error is None
