@@ -44,7 +44,7 @@ METRIC = "pair-solves/s (batched serving, 512-request mixed stream)"
 # capture of the kernel with 64 pairs of the stream active
 # (dram__bytes_read.sum + dram__bytes_write.sum over the launch's vertices);
 # the traffic grows in proportion to the vertices stepped.
-TRAFFIC_BYTES_PER_VERTEX = (229.956608e6 + 43.097088e6) / 1638986
+TRAFFIC_BYTES_PER_VERTEX = (229.997312e6 + 44.046080e6) / 1638986
 UNIT = "pair-solves/s"
 WORKLOAD = "serving-stream-512 (V logU[2k,100k], T logU[5k,500k], N 64|128, 500 steps)"
 
