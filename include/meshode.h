@@ -118,8 +118,9 @@ typedef struct MoDfOptions {
     int32_t method;   /* MO_DF_AUTO, MO_DF_BRUTE or MO_DF_LBVH */
     int32_t packet;   /* MO_PACKET_* for MO_DF_LBVH */
     float band;       /* 0: exact grid.  > 0: voxels at distance >= band store
-                       * band, except the two lowest layers along each axis
-                       * (x, y or z <= 1), which stay exact; see mo_df_loss_band */
+                       * band, except in the two lowest layers along each axis
+                       * (x, y or z <= 1), whose band is band + 13/N; see
+                       * mo_df_loss_band */
     int32_t reserved; /* 0 */
 } MoDfOptions;
 /* mo_df_build with explicit build options (opt == NULL: defaults).  method
@@ -132,15 +133,21 @@ int mo_df_build_ex(const float* V, int64_t nv, const int32_t* F, int64_t nf, int
  * 147-148) returns 0 when the in-range trilinear value exceeds 0.2; grid
  * values are 1-Lipschitz, so a cell with a corner at or beyond the band has
  * every corner above 0.2 + 1e-3 - rounding and interpolates above 0.2 from
- * either grid, and the only lookups that extrapolate (coordinates in
- * (-1/N, 0)) read the exact lowest layers.  The serving pool builds with this
- * band: its losses and results are bit-identical to an exact grid's, and the
- * build skips most of the far field. */
+ * either grid.  The only lookups that extrapolate (coordinates in (-1/N, 0))
+ * read cells whose 8 corners all lie in the two lowest layers of an axis;
+ * there, with corners 1/N apart differing by at most 1/N, each extrapolated
+ * axis (weights in (-1, 0)) lowers the value by at most the spread of its
+ * inputs and triples their spread, so the value is at least the smallest
+ * corner minus (1 + 3 + 9)/N, and those layers use band + 13/N.  The
+ * serving pool builds with this band: its losses and results are
+ * bit-identical to an exact grid's, and the build skips most of the far
+ * field. */
 float mo_df_loss_band(int N);
 /* The target's traversal tree alone, for on-demand fills (mo_df_lazy_fill):
  * the steps of the LBVH build of mo_df_build_ex without the grid pass.
  * tree_out (mo_df_tree_bytes(nf) bytes, 16-byte aligned) gets the sorted
- * triangle records, then the internal nodes' traversal records.  scratch:
+ * triangle records (80 B each), then the internal nodes' traversal records
+ * (144 B each).  scratch:
  * mo_df_tree_scratch_bytes; status_out (device int32) gets bit 1 for a face
  * index out of range.  Nothing is synchronised. */
 size_t mo_df_tree_bytes(int64_t nf);

@@ -104,15 +104,23 @@ __device__ __forceinline__ float dotf3(float3 a, float x, float y, float z) {
     return fmaf(a.z, z, fmaf(a.y, y, __fmul_rn(a.x, x)));
 }
 
+// Traversal record of an internal node: NODE_F4 float4, per child (left,
+// then right) (o.xyz, e.x) (a1.xyz, e.y) (a2.xyz, e.z) (a3.xyz, id), then
+// (left count, right count, 0, 0) as ints.  o: the box's origin corner,
+// a1..a3 its axes (a3 = obb_a3(a1, a2), stored so the walk does not
+// recompute it), e its extents; id >= 0 an internal node, ~first for a
+// bucket of `count` (1..DF_BUCKET) sorted triangles (count 0: internal).
+constexpr int NODE_F4 = 9;
+
 // Squared distance from p to a child's box (the bound the traversal uses).
 __device__ __forceinline__ float obb_d2(float px, float py, float pz, float4 g0, float4 g1, float4 g2, float4 g3) {
     const float qx = __fsub_rn(px, g0.x), qy = __fsub_rn(py, g0.y), qz = __fsub_rn(pz, g0.z);
     const float3 a1 = make_float3(g1.x, g1.y, g1.z), a2 = make_float3(g2.x, g2.y, g2.z);
-    const float3 a3 = obb_a3(a1, a2);
+    const float3 a3 = make_float3(g3.x, g3.y, g3.z);
     const float t1 = dotf3(a1, qx, qy, qz), t2 = dotf3(a2, qx, qy, qz), t3 = dotf3(a3, qx, qy, qz);
-    const float s1 = fmaxf(fmaxf(-t1, t1 - g2.w), 0.f);
-    const float s2 = fmaxf(fmaxf(-t2, t2 - g3.x), 0.f);
-    const float s3 = fmaxf(fmaxf(-t3, t3 - g3.y), 0.f);
+    const float s1 = fmaxf(fmaxf(-t1, t1 - g0.w), 0.f);
+    const float s2 = fmaxf(fmaxf(-t2, t2 - g1.w), 0.f);
+    const float s3 = fmaxf(fmaxf(-t3, t3 - g2.w), 0.f);
     return s1 * s1 + s2 * s2 + s3 * s3;
 }
 
@@ -133,8 +141,27 @@ constexpr int TRAV_STACK = 64;
 // launch: MO_PACKET_4x4x2 (default), 8x4x1, 4x2x4, 2x4x4, 8x2x2.
 // Band: with band > 0 a voxel whose distance is not below `band` stores
 // `band` itself, except in the two lowest layers along each axis (x, y or
-// z <= 1), which stay exact everywhere; band2 = band^2 (FLT_MAX for none).
-__device__ __forceinline__ bool exact_layer(int x, int y, int z) { return x <= 1 || y <= 1 || z <= 1; }
+// z <= 1), where lookups just below the cube extrapolate: there the band is
+// band + 13/N; band2 = band^2 (FLT_MAX for none).
+struct VoxelBand {
+    float bound2;  // squared distance a triangle must beat (FLT_MAX: none)
+    float value;   // stored when none does
+};
+
+__device__ __forceinline__ VoxelBand voxel_band(int x, int y, int z, int N, float band, float band2) {
+    VoxelBand b;
+    if (band2 == FLT_MAX) {
+        b.bound2 = FLT_MAX;
+        b.value = 0.f;
+    } else if (x <= 1 || y <= 1 || z <= 1) {
+        b.value = __fadd_rn(band, __fdiv_rn(13.0f, (float)N));
+        b.bound2 = __fmul_rn(b.value, b.value);
+    } else {
+        b.bound2 = band2;
+        b.value = band;
+    }
+    return b;
+}
 
 // The value the voxel (x, y, z) of this lane stores: its exact distance to
 // the nearest triangle, or `band` when that is not below the band.  All 32
@@ -147,7 +174,8 @@ __device__ __forceinline__ float df_voxel_value(const float4* __restrict__ nodes
     const int lane = threadIdx.x & 31;
     const float Nf = (float)N;
     const float px = __fdiv_rn((float)x, Nf), py = __fdiv_rn((float)y, Nf), pz = __fdiv_rn((float)z, Nf);
-    const float init = exact_layer(x, y, z) ? FLT_MAX : band2;
+    const VoxelBand vb = voxel_band(x, y, z, N, band, band2);
+    const float init = vb.bound2;
     float best = valid ? init : -1.0f;
     // Boxes are visited while their fp32 distance is within kSlack (in
     // distance units) of the lane's best: the rounding of the box bound can
@@ -172,11 +200,12 @@ __device__ __forceinline__ float df_voxel_value(const float4* __restrict__ nodes
                 if (lane == 0) atomicOr(status, 4);
                 break;
             }
-            const float4* nd = nodes + 8 * (int64_t)node;
+            const float4* nd = nodes + NODE_F4 * (int64_t)node;
             const float4 l0 = __ldg(nd), l1 = __ldg(nd + 1), l2 = __ldg(nd + 2), l3 = __ldg(nd + 3);
             const float4 r0 = __ldg(nd + 4), r1 = __ldg(nd + 5), r2 = __ldg(nd + 6), r3 = __ldg(nd + 7);
-            const int L = __float_as_int(l0.w), R = __float_as_int(r0.w);
-            const int cl = __float_as_int(l1.w), cr = __float_as_int(r1.w);  // bucket sizes (0: internal)
+            const int2 cnt = __ldg(reinterpret_cast<const int2*>(nd + 8));
+            const int L = __float_as_int(l3.w), R = __float_as_int(r3.w);
+            const int cl = cnt.x, cr = cnt.y;  // bucket sizes (0: internal)
             const float dl = obb_d2(px, py, pz, l0, l1, l2, l3), dr = obb_d2(px, py, pz, r0, r1, r2, r3);
             bool wl = __any_sync(FULL, dl < lim);
             bool wr = __any_sync(FULL, dr < lim);
@@ -213,7 +242,7 @@ __device__ __forceinline__ float df_voxel_value(const float4* __restrict__ nodes
             __syncwarp();
         }
     }
-    return best < band2 || init == FLT_MAX ? __fsqrt_rn(best) : band;
+    return best < init ? __fsqrt_rn(best) : vb.value;
 }
 
 }  // namespace mo

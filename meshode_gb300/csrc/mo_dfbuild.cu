@@ -496,15 +496,13 @@ __global__ void k_obb_walk(const float4* __restrict__ nodes, const int2* __restr
     }
 }
 
-// Traversal records, 8 float4 per internal node, per child (left then right):
-//   (o.xyz, id) (a1.xyz, count) (a2.xyz, e.x) (e.y, e.z, 0, 0)
-// id >= 0 an internal node, ~first for a bucket of `count` (1..DF_BUCKET)
-// sorted triangles.
+// Traversal records (layout at NODE_F4 in mo_df_trav.cuh).
 __global__ void k_obb_nodes(const float4* __restrict__ nodes, const int2* __restrict__ range, int n,
                             const float4* __restrict__ tris, const float4* __restrict__ obb,
                             float4* __restrict__ tnodes) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
+    int cnts[2];
     for (int side = 0; side < 2; ++side) {
         const int c = __float_as_int(nodes[4 * (int64_t)i + side].w);
         int id = c, cnt = 0;
@@ -521,12 +519,15 @@ __global__ void k_obb_nodes(const float4* __restrict__ nodes, const int2* __rest
                 cnt = r.y - r.x + 1;
             }
         }
-        float4* t = tnodes + 8 * (int64_t)i + 4 * side;
-        t[0] = make_float4(b.o.x, b.o.y, b.o.z, __int_as_float(id));
-        t[1] = make_float4(b.a1.x, b.a1.y, b.a1.z, __int_as_float(cnt));
-        t[2] = make_float4(b.a2.x, b.a2.y, b.a2.z, b.e.x);
-        t[3] = make_float4(b.e.y, b.e.z, 0.f, 0.f);
+        const float3 a3 = obb_a3(b.a1, b.a2);
+        float4* t = tnodes + NODE_F4 * (int64_t)i + 4 * side;
+        t[0] = make_float4(b.o.x, b.o.y, b.o.z, b.e.x);
+        t[1] = make_float4(b.a1.x, b.a1.y, b.a1.z, b.e.y);
+        t[2] = make_float4(b.a2.x, b.a2.y, b.a2.z, b.e.z);
+        t[3] = make_float4(a3.x, a3.y, a3.z, __int_as_float(id));
+        cnts[side] = cnt;
     }
+    tnodes[NODE_F4 * (int64_t)i + 8] = make_float4(__int_as_float(cnts[0]), __int_as_float(cnts[1]), 0.f, 0.f);
 }
 
 // The full grid: one warp per packet of PX x PY x PZ voxels.
@@ -580,7 +581,8 @@ __global__ void __launch_bounds__(BF_THREADS) k_df_brute(const float4* __restric
     const int x = (int)(v % N), y = (int)((v / N) % N), z = (int)(v / ((int64_t)N * N));
     const float Nf = (float)N;
     const float px = __fdiv_rn((float)x, Nf), py = __fdiv_rn((float)y, Nf), pz = __fdiv_rn((float)z, Nf);
-    const float init = exact_layer(x, y, z) ? FLT_MAX : band2;
+    const VoxelBand vb = voxel_band(x, y, z, N, band, band2);
+    const float init = vb.bound2;
     float best = init;
     for (int base = 0; base < ntri; base += BF_CHUNK) {
         const int cnt = min(BF_CHUNK, ntri - base);
@@ -594,7 +596,7 @@ __global__ void __launch_bounds__(BF_THREADS) k_df_brute(const float4* __restric
             best = fminf(best, tri_d2(px, py, pz, T, valid ? best : -1.0f));
         }
     }
-    if (valid) grid[v] = best < band2 || init == FLT_MAX ? __fsqrt_rn(best) : band;
+    if (valid) grid[v] = best < init ? __fsqrt_rn(best) : vb.value;
 }
 
 // ---------------------------------------------------------------------------
@@ -616,7 +618,7 @@ struct BuildScratch {
     int* status;
     int2* range;    // leaves [first, last] of every internal node
     float4* obb;    // 4 float4 per internal node: its oriented box and normal sum
-    float4* tnodes; // 8 float4 per internal node: the traversal records
+    float4* tnodes; // NODE_F4 float4 per internal node: the traversal records
     size_t bytes;
 };
 
@@ -646,7 +648,7 @@ static BuildScratch plan_scratch(char* base, int64_t nv, int64_t nf, int method)
         s.hist = reinterpret_cast<int*>(take(sizeof(int) * radix_hist_ints((int)nf)));
         s.range = reinterpret_cast<int2*>(take(sizeof(int2) * (size_t)(nf > 1 ? nf - 1 : 1)));
         s.obb = reinterpret_cast<float4*>(take(sizeof(float4) * 4 * (size_t)(nf > 1 ? nf - 1 : 1)));
-        s.tnodes = reinterpret_cast<float4*>(take(sizeof(float4) * 8 * (size_t)(nf > 1 ? nf - 1 : 1)));
+        s.tnodes = reinterpret_cast<float4*>(take(sizeof(float4) * NODE_F4 * (size_t)(nf > 1 ? nf - 1 : 1)));
     } else {
         s.codes_a = s.codes_b = nullptr;
         s.ids_a = s.ids_b = nullptr;
@@ -688,7 +690,7 @@ using namespace mo;
 
 extern "C" size_t mo_df_tree_bytes(int64_t nf) {
     if (nf <= 0) return 0;
-    return sizeof(float4) * ((size_t)TRI_F4 * nf + 8 * (size_t)(nf > 1 ? nf - 1 : 1));
+    return sizeof(float4) * ((size_t)TRI_F4 * nf + NODE_F4 * (size_t)(nf > 1 ? nf - 1 : 1));
 }
 
 extern "C" size_t mo_df_tree_scratch_bytes(int64_t nv, int64_t nf) {

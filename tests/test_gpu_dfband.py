@@ -1,9 +1,9 @@
 """The loss-preserving distance-field band (MoDfOptions.band,
 mo_df_loss_band) on the GPU.
 
-* Grid: voxels below the band and the two lowest layers along each axis
-  hold exactly the exact build's value; every other voxel holds the band.
-  The same for both methods and every packet shape.
+* Grid: voxels below the band hold exactly the exact build's value, every
+  other voxel holds the band; in the two lowest layers along each axis the
+  band is band + 13/N.  The same for both methods and every packet shape.
 * DistanceFieldLoss forward and backward (UniformGrid::DistanceFloat through
   the jet, uniformgrid.cc:120-185) from the banded grid equal, bit for bit,
   those from the exact grid at points everywhere: inside the cube, near the
@@ -72,7 +72,8 @@ def test_band_grid(cuda, name, N):
     exact, _ = _build(V, F, N, L.MO_DF_LBVH, L.MO_PACKET_4x4x2, 0.0)
     exact = exact.cpu().numpy()
     low = _low_layers(N)
-    keep = low | (exact < np.float32(band))
+    wide = np.float32(band) + np.float32(13.0) / np.float32(N)
+    keep = (low & (exact < wide)) | (~low & (exact < np.float32(band)))
     assert (~keep).any() and keep.any()
     for method, packets in ((L.MO_DF_BRUTE, [L.MO_PACKET_4x4x2]),
                             (L.MO_DF_LBVH, [L.MO_PACKET_4x4x2, L.MO_PACKET_8x4x1, L.MO_PACKET_4x2x4,
@@ -81,7 +82,8 @@ def test_band_grid(cuda, name, N):
             g, _ = _build(V, F, N, method, packet, band)
             g = g.cpu().numpy()
             assert np.array_equal(g[keep], exact[keep]), (method, packet)
-            assert np.all(g[~keep] == np.float32(band)), (method, packet)
+            assert np.all(g[~keep & ~low] == np.float32(band)), (method, packet)
+            assert np.all(g[~keep & low] == wide), (method, packet)
 
 
 def _probes(N, Vn, n=40000, seed=5):
