@@ -114,6 +114,12 @@ size_t mo_df_noalloc_scratch_capacity(void);
 #define MO_PACKET_4x2x4 2
 #define MO_PACKET_2x4x4 3
 #define MO_PACKET_8x2x2 4
+/* Two voxels per lane (64 per warp, the second one PZ further along z),
+ * evaluated with packed FP32 math: bases 4x4x2, 2x4x4 and 8x4x1. */
+#define MO_PACKET_4x4x4 5
+#define MO_PACKET_2x4x8 6
+#define MO_PACKET_8x4x2 7
+#define MO_PACKET_LAST 7
 typedef struct MoDfOptions {
     int32_t method;   /* MO_DF_AUTO, MO_DF_BRUTE or MO_DF_LBVH */
     int32_t packet;   /* MO_PACKET_* for MO_DF_LBVH */

@@ -245,4 +245,172 @@ __device__ __forceinline__ float df_voxel_value(const float4* __restrict__ nodes
     return best < init ? __fsqrt_rn(best) : vb.value;
 }
 
+// ---------------------------------------------------------------------------
+// Two voxels per lane, on the packed FP32 pipe (FFMA2 / FADD2 / FMUL2 of
+// sm_100+): one walk of the tree serves 64 voxels, the node and triangle
+// loads, votes and stack are shared, and every per-voxel operation is the
+// same IEEE operation as in the one-voxel code, in the same order, so each
+// voxel gets the same value bit for bit.  Subtracting a uniform scalar is
+// written as adding its negation (a - b == a + (-b) exactly), and
+// fmaf(-t, b, x) as fma(t, -b, x) (the same exact product).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 bc2(float s) { return make_float2(s, s); }
+
+__device__ __forceinline__ float2 dot3e2(float2 ax, float2 ay, float2 az, float bx, float by, float bz) {
+    return __ffma2_rn(az, bc2(bz), __ffma2_rn(ay, bc2(by), __fmul2_rn(ax, bc2(bx))));
+}
+
+__device__ __forceinline__ float2 dot3e2(float2 ax, float2 ay, float2 az) {
+    return __ffma2_rn(az, az, __ffma2_rn(ay, ay, __fmul2_rn(ax, ax)));
+}
+
+__device__ __forceinline__ float2 clamp01_2(float2 t) {
+    return make_float2(fminf(fmaxf(t.x, 0.f), 1.f), fminf(fmaxf(t.y, 0.f), 1.f));
+}
+
+__device__ __forceinline__ float2 fmin2(float2 a, float2 b) { return make_float2(fminf(a.x, b.x), fminf(a.y, b.y)); }
+
+__device__ __forceinline__ float2 seg3_d2_2(float2 px, float2 py, float2 pz, float4 a, float4 b, float inv_l2) {
+    const float ex = __fsub_rn(b.x, a.x), ey = __fsub_rn(b.y, a.y), ez = __fsub_rn(b.z, a.z);
+    const float2 apx = __fadd2_rn(px, bc2(-a.x)), apy = __fadd2_rn(py, bc2(-a.y)), apz = __fadd2_rn(pz, bc2(-a.z));
+    const float2 t = clamp01_2(__fmul2_rn(dot3e2(apx, apy, apz, ex, ey, ez), bc2(inv_l2)));
+    const float2 qx = __ffma2_rn(t, bc2(-ex), apx), qy = __ffma2_rn(t, bc2(-ey), apy),
+                 qz = __ffma2_rn(t, bc2(-ez), apz);
+    return dot3e2(qx, qy, qz);
+}
+
+// tri_d2 for two points; the plane-distance cull skips the rest when no
+// voxel of the warp can beat its best.
+__device__ __forceinline__ float2 tri_d2_2(float2 px, float2 py, float2 pz, const Tri& T, float2 cut) {
+    if (T.r3.w != 0.f) {
+        const float2 qx = __fadd2_rn(px, bc2(-T.r0.x)), qy = __fadd2_rn(py, bc2(-T.r0.y)),
+                     qz = __fadd2_rn(pz, bc2(-T.r0.z));
+        const float2 h = dot3e2(qx, qy, qz, T.r3.x, T.r3.y, T.r3.z);
+        const float2 h2 = __fmul2_rn(h, h);
+        if (!__any_sync(0xffffffffu, h2.x < cut.x || h2.y < cut.y)) return bc2(FLT_MAX);
+        const float2 x = dot3e2(qx, qy, qz, T.r1.x, T.r1.y, T.r1.z);
+        const float2 y = dot3e2(qx, qy, qz, T.r2.x, T.r2.y, T.r2.z);
+        const float bx = T.r0.w, cx = T.r1.w, cy = T.r2.w, ebx = T.r4.w;
+        const float2 y2 = __fmul2_rn(y, y);
+        // A-B along the x axis
+        float2 t = clamp01_2(__fmul2_rn(x, bc2(T.r4.x)));
+        float2 dx = __ffma2_rn(t, bc2(-bx), x);
+        float2 d = __ffma2_rn(dx, dx, y2);
+        // A-C
+        t = clamp01_2(__fmul2_rn(__ffma2_rn(x, bc2(cx), __fmul2_rn(y, bc2(cy))), bc2(T.r4.y)));
+        dx = __ffma2_rn(t, bc2(-cx), x);
+        float2 dy = __ffma2_rn(t, bc2(-cy), y);
+        d = fmin2(d, __ffma2_rn(dx, dx, __fmul2_rn(dy, dy)));
+        // B-C
+        const float2 xb = __fadd2_rn(x, bc2(-bx));
+        t = clamp01_2(__fmul2_rn(__ffma2_rn(xb, bc2(ebx), __fmul2_rn(y, bc2(cy))), bc2(T.r4.z)));
+        dx = __ffma2_rn(t, bc2(-ebx), xb);
+        dy = __ffma2_rn(t, bc2(-cy), y);
+        d = fmin2(d, __ffma2_rn(dx, dx, __fmul2_rn(dy, dy)));
+        // inside: left of A->B, B->C and C->A
+        const float2 sb = __ffma2_rn(bc2(ebx), y, __fmul2_rn(bc2(-cy), xb));
+        const float2 sc = __ffma2_rn(bc2(cy), x, __fmul2_rn(bc2(-cx), y));
+        const float2 hd = __fadd2_rn(h2, d);
+        const bool inx = (y.x >= 0.f) && (sb.x >= 0.f) && (sc.x >= 0.f);
+        const bool iny = (y.y >= 0.f) && (sb.y >= 0.f) && (sc.y >= 0.f);
+        return make_float2(inx ? h2.x : hd.x, iny ? h2.y : hd.y);
+    }
+    float2 d = seg3_d2_2(px, py, pz, T.r0, T.r1, T.r4.x);
+    d = fmin2(d, seg3_d2_2(px, py, pz, T.r1, T.r2, T.r4.y));
+    d = fmin2(d, seg3_d2_2(px, py, pz, T.r2, T.r0, T.r4.z));
+    return d;
+}
+
+// obb_d2 for two points (a bound only: its rounding may differ from the
+// one-point form by a few ulps, far inside the traversal's slack).
+__device__ __forceinline__ float2 obb_d2_2(float2 px, float2 py, float2 pz, float4 g0, float4 g1, float4 g2,
+                                           float4 g3) {
+    const float2 qx = __fadd2_rn(px, bc2(-g0.x)), qy = __fadd2_rn(py, bc2(-g0.y)), qz = __fadd2_rn(pz, bc2(-g0.z));
+    const float2 t1 = dot3e2(qx, qy, qz, g1.x, g1.y, g1.z);
+    const float2 t2 = dot3e2(qx, qy, qz, g2.x, g2.y, g2.z);
+    const float2 t3 = dot3e2(qx, qy, qz, g3.x, g3.y, g3.z);
+    const float2 u1 = __fadd2_rn(t1, bc2(-g0.w)), u2 = __fadd2_rn(t2, bc2(-g1.w)), u3 = __fadd2_rn(t3, bc2(-g2.w));
+    const float2 s1 = make_float2(fmaxf(fmaxf(-t1.x, u1.x), 0.f), fmaxf(fmaxf(-t1.y, u1.y), 0.f));
+    const float2 s2 = make_float2(fmaxf(fmaxf(-t2.x, u2.x), 0.f), fmaxf(fmaxf(-t2.y, u2.y), 0.f));
+    const float2 s3 = make_float2(fmaxf(fmaxf(-t3.x, u3.x), 0.f), fmaxf(fmaxf(-t3.y, u3.y), 0.f));
+    return dot3e2(s1, s2, s3);
+}
+
+// The values of voxels (x, y, za) and (x, y, zb) of this lane, by one joint
+// walk of the warp (see df_voxel_value).
+__device__ __forceinline__ float2 df_voxel_value2(const float4* __restrict__ nodes,
+                                                  const float4* __restrict__ tris, int ntri, int N, float band,
+                                                  float band2, int x, int y, int za, int zb, bool va, bool vb,
+                                                  int* stack, int* __restrict__ status) {
+    const int lane = threadIdx.x & 31;
+    const float Nf = (float)N;
+    const float fx = __fdiv_rn((float)x, Nf), fy = __fdiv_rn((float)y, Nf);
+    const float2 px = bc2(fx), py = bc2(fy);
+    const float2 pz = make_float2(__fdiv_rn((float)za, Nf), __fdiv_rn((float)zb, Nf));
+    const VoxelBand ba = voxel_band(x, y, za, N, band, band2), bb = voxel_band(x, y, zb, N, band, band2);
+    const float2 init = make_float2(ba.bound2, bb.bound2);
+    float2 best = make_float2(va ? init.x : -1.0f, vb ? init.y : -1.0f);
+    float2 lim = make_float2(va ? (init.x == FLT_MAX ? FLT_MAX : slack_bound(init.x)) : -1.0f,
+                             vb ? (init.y == FLT_MAX ? FLT_MAX : slack_bound(init.y)) : -1.0f);
+    const unsigned FULL = 0xffffffffu;
+    if (ntri == 1) {
+        const float2 t = tri_d2_2(px, py, pz, load_tri(tris, 0), best);
+        if (va && t.x < best.x) best.x = t.x;
+        if (vb && t.y < best.y) best.y = t.y;
+    } else {
+        int sp = 0;
+        int node = 0;
+        const int64_t max_iter = 2 * (int64_t)ntri + 64;
+        for (int64_t iter = 0;; ++iter) {
+            if (iter > max_iter) {
+                if (lane == 0) atomicOr(status, 4);
+                break;
+            }
+            const float4* nd = nodes + NODE_F4 * (int64_t)node;
+            const float4 l0 = __ldg(nd), l1 = __ldg(nd + 1), l2 = __ldg(nd + 2), l3 = __ldg(nd + 3);
+            const float4 r0 = __ldg(nd + 4), r1 = __ldg(nd + 5), r2 = __ldg(nd + 6), r3 = __ldg(nd + 7);
+            const int2 cnt = __ldg(reinterpret_cast<const int2*>(nd + 8));
+            const int L = __float_as_int(l3.w), R = __float_as_int(r3.w);
+            const int cl = cnt.x, cr = cnt.y;
+            const float2 dl = obb_d2_2(px, py, pz, l0, l1, l2, l3), dr = obb_d2_2(px, py, pz, r0, r1, r2, r3);
+            bool wl = __any_sync(FULL, dl.x < lim.x || dl.y < lim.y);
+            bool wr = __any_sync(FULL, dr.x < lim.x || dr.y < lim.y);
+            const int nl = wl ? cl : 0, nr = wr ? cr : 0;
+#pragma unroll 1
+            for (int k = 0; k < nl + nr; ++k) {
+                const int tri = k < nl ? ~L + k : ~R + (k - nl);
+                const float2 t = tri_d2_2(px, py, pz, load_tri(tris, tri), best);
+                if (va && t.x < best.x) { best.x = t.x; lim.x = slack_bound(best.x); }
+                if (vb && t.y < best.y) { best.y = t.y; lim.y = slack_bound(best.y); }
+            }
+            if (cl > 0) wl = false;
+            if (cr > 0) wr = false;
+            if (wl && wr) {
+                // nearer child first by majority over the warp's voxels
+                const unsigned na = __ballot_sync(FULL, va && dl.x <= dr.x);
+                const unsigned nb = __ballot_sync(FULL, vb && dl.y <= dr.y);
+                const unsigned aa = __ballot_sync(FULL, va), ab = __ballot_sync(FULL, vb);
+                const bool lfirst = 2 * (__popc(na) + __popc(nb)) >= __popc(aa) + __popc(ab);
+                if (sp >= TRAV_STACK) {
+                    if (lane == 0) atomicOr(status, 2);
+                    break;
+                }
+                if (lane == 0) stack[sp] = lfirst ? R : L;
+                ++sp;
+                node = lfirst ? L : R;
+            } else if (wl) {
+                node = L;
+            } else if (wr) {
+                node = R;
+            } else {
+                if (sp == 0) break;
+                __syncwarp();
+                node = stack[--sp];
+            }
+            __syncwarp();
+        }
+    }
+    return make_float2(best.x < init.x ? __fsqrt_rn(best.x) : ba.value, best.y < init.y ? __fsqrt_rn(best.y) : bb.value);
+}
+
 }  // namespace mo

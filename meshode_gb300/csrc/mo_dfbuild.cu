@@ -549,6 +549,36 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) k_df_lbvh(const float4* __res
     if (valid) grid[((int64_t)z * N + y) * N + x] = v;
 }
 
+// Two voxels per lane: the base packet PX x PY x PZ and the one PZ above it.
+template <int PX, int PY, int PZ>
+__global__ void __launch_bounds__(TRAV_WARPS * 32) k_df_lbvh2(const float4* __restrict__ nodes,
+                                                              const float4* __restrict__ tris, int ntri, int N,
+                                                              float band, float band2, float* __restrict__ grid,
+                                                              int* __restrict__ status) {
+    __shared__ int stack[TRAV_WARPS][TRAV_STACK];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    static_assert(PX * PY * PZ == 32, "a packet is one warp");
+    const int bx = (N + PX - 1) / PX, by = (N + PY - 1) / PY, bz = (N + 2 * PZ - 1) / (2 * PZ);
+    const int64_t brick = (int64_t)blockIdx.x * TRAV_WARPS + w;
+    if (brick >= (int64_t)bx * by * bz) return;  // warp-uniform
+    const int ix = (int)(brick % bx), iy = (int)((brick / bx) % by), iz = (int)(brick / ((int64_t)bx * by));
+    const int x = ix * PX + (lane % PX), y = iy * PY + ((lane / PX) % PY);
+    const int za = iz * 2 * PZ + lane / (PX * PY), zb = za + PZ;
+    const bool va = x < N && y < N && za < N, vb = x < N && y < N && zb < N;
+    const float2 v = df_voxel_value2(nodes, tris, ntri, N, band, band2, x, y, za, zb, va, vb, stack[w], status);
+    if (va) grid[((int64_t)za * N + y) * N + x] = v.x;
+    if (vb) grid[((int64_t)zb * N + y) * N + x] = v.y;
+}
+
+template <int PX, int PY, int PZ>
+static void launch_df_lbvh2_shape(const float4* nodes, const float4* tris, int ntri, int N, float band, float band2,
+                                  float* grid, int* status, cudaStream_t s) {
+    const int64_t bricks = (int64_t)((N + PX - 1) / PX) * ((N + PY - 1) / PY) * ((N + 2 * PZ - 1) / (2 * PZ));
+    k_df_lbvh2<PX, PY, PZ><<<ceil_div(bricks, TRAV_WARPS), TRAV_WARPS * 32, 0, s>>>(nodes, tris, ntri, N, band,
+                                                                                  band2, grid, status);
+    ::mo::note_launch();
+}
+
 template <int PX, int PY, int PZ>
 static void launch_df_lbvh_shape(const float4* nodes, const float4* tris, int ntri, int N, float band, float band2,
                                  float* grid, int* status, cudaStream_t s) {
@@ -565,6 +595,9 @@ static void launch_df_lbvh(int packet, const float4* nodes, const float4* tris, 
         case MO_PACKET_4x2x4: launch_df_lbvh_shape<4, 2, 4>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
         case MO_PACKET_2x4x4: launch_df_lbvh_shape<2, 4, 4>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
         case MO_PACKET_8x2x2: launch_df_lbvh_shape<8, 2, 2>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
+        case MO_PACKET_4x4x4: launch_df_lbvh2_shape<4, 4, 2>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
+        case MO_PACKET_2x4x8: launch_df_lbvh2_shape<2, 4, 4>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
+        case MO_PACKET_8x4x2: launch_df_lbvh2_shape<8, 4, 1>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
         default: launch_df_lbvh_shape<4, 4, 2>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
     }
 }
@@ -776,7 +809,7 @@ extern "C" int mo_df_build_ex(const float* V, int64_t nv, const int32_t* F, int6
     int method = opt ? opt->method : MO_DF_AUTO;
     const int packet = opt ? opt->packet : MO_PACKET_4x4x2;
     const float band = opt ? opt->band : 0.0f;
-    MO_CHECK_ARG(packet >= MO_PACKET_4x4x2 && packet <= MO_PACKET_8x2x2, "unknown packet shape %d", packet);
+    MO_CHECK_ARG(packet >= MO_PACKET_4x4x2 && packet <= MO_PACKET_LAST, "unknown packet shape %d", packet);
     MO_CHECK_ARG(band >= 0.0f && band <= 4.0f, "band must be in [0, 4] (0: exact grid), got %g", (double)band);
     const float band2 = band > 0.0f ? band * band : FLT_MAX;
     MO_CHECK_ARG(nv > 0 && nf > 0, "target mesh must have vertices and faces (nv=%lld nf=%lld)", (long long)nv,

@@ -768,7 +768,7 @@ extern "C" int mo_pool_submit(MoPool* P, const MoRequest* q, int64_t* id_out) {
                                                                             : P->cfg.slices_per_tile;
     MO_CHECK_ARG(q->df_method == MO_DF_AUTO || q->df_method == MO_DF_BRUTE || q->df_method == MO_DF_LBVH,
                  "unknown DF method %d", q->df_method);
-    MO_CHECK_ARG(q->df_packet >= MO_PACKET_4x4x2 && q->df_packet <= MO_PACKET_8x2x2, "unknown packet %d",
+    MO_CHECK_ARG(q->df_packet >= MO_PACKET_4x4x2 && q->df_packet <= MO_PACKET_LAST, "unknown packet %d",
                  q->df_packet);
     R->method = q->df_method == MO_DF_AUTO ? mo_df_method_for(q->ntf, q->N) : q->df_method;
     R->packet = q->df_packet;

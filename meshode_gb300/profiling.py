@@ -18,7 +18,7 @@ import torch
 
 from . import _lib as L
 from . import build as B
-from . import meshgen, serving
+from . import autotune, meshgen, serving
 
 
 def _stream(n, seed=5):
@@ -86,7 +86,7 @@ def main(argv=None):
     b.add_argument("--repeat", type=int, default=2)
     b.add_argument("--method", default="auto", choices=["auto", "brute", "lbvh"])
     b.add_argument("--band", action="store_true")
-    b.add_argument("--packet", default="4x4x2", choices=["4x4x2", "8x4x1", "4x2x4", "2x4x4", "8x2x2"])
+    b.add_argument("--packet", default="4x4x2", choices=list(autotune.PACKETS))
     args = ap.parse_args(argv)
     B.build()
     L.require_cuda()

@@ -77,7 +77,8 @@ def test_band_grid(cuda, name, N):
     assert (~keep).any() and keep.any()
     for method, packets in ((L.MO_DF_BRUTE, [L.MO_PACKET_4x4x2]),
                             (L.MO_DF_LBVH, [L.MO_PACKET_4x4x2, L.MO_PACKET_8x4x1, L.MO_PACKET_4x2x4,
-                                            L.MO_PACKET_2x4x4, L.MO_PACKET_8x2x2])):
+                                            L.MO_PACKET_2x4x4, L.MO_PACKET_8x2x2, L.MO_PACKET_4x4x4,
+                                            L.MO_PACKET_2x4x8, L.MO_PACKET_8x4x2])):
         for packet in packets:
             g, _ = _build(V, F, N, method, packet, band)
             g = g.cpu().numpy()
