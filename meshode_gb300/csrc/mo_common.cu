@@ -33,40 +33,64 @@ int device_sm_count() {
 }
 
 // ---------------------------------------------------------------------------
-// Single-CTA exclusive scan: 1024 threads, each owns a contiguous chunk.
+// Single-CTA exclusive scan, in tiles of 1024 x 8 ints: coalesced loads into
+// shared memory, each thread scans 8 consecutive ints, a block scan of the
+// thread sums, coalesced stores; a running carry joins the tiles.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(1024) k_scan_1cta(int* a, int n, int* total) {
+constexpr int SCAN_THREADS = 1024, SCAN_PER = 8, SCAN_TILE = SCAN_THREADS * SCAN_PER;
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_1cta(int* a, int n, int* total) {
+    __shared__ int tile[SCAN_TILE + SCAN_TILE / 32];  // one pad int per 32 breaks bank conflicts
     __shared__ int warp_sums[32];
-    const int tid = threadIdx.x;
-    const int chunk = (n + 1023) / 1024;
-    const int beg = min(n, tid * chunk), end = min(n, beg + chunk);
-    int s = 0;
-    for (int i = beg; i < end; ++i) s += a[i];
-    // block exclusive scan of s
-    const int lane = tid & 31, w = tid >> 5;
-    int x = s;
-    for (int o = 1; o < 32; o <<= 1) {
-        int y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) warp_sums[w] = x;
-    __syncthreads();
-    if (w == 0) {
-        int ws = warp_sums[lane];
-        for (int o = 1; o < 32; o <<= 1) {
-            int y = __shfl_up_sync(0xffffffffu, ws, o);
-            if (lane >= o) ws += y;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    auto at = [](int i) { return i + (i >> 5); };
+    int carry = 0;
+    for (int base = 0; base < n; base += SCAN_TILE) {
+#pragma unroll
+        for (int k = 0; k < SCAN_PER; ++k) {
+            const int i = k * SCAN_THREADS + tid;
+            tile[at(i)] = base + i < n ? a[base + i] : 0;
         }
-        warp_sums[lane] = ws;  // inclusive
+        __syncthreads();
+        int v[SCAN_PER];
+        int s = 0;
+#pragma unroll
+        for (int k = 0; k < SCAN_PER; ++k) {
+            v[k] = s;
+            s += tile[at(tid * SCAN_PER + k)];
+        }
+        int x = s;  // inclusive scan of the thread sums
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_sums[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            int ws = warp_sums[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, ws, o);
+                if (lane >= o) ws += y;
+            }
+            warp_sums[lane] = ws;
+        }
+        __syncthreads();
+        const int pre = carry + x - s + (w > 0 ? warp_sums[w - 1] : 0);
+#pragma unroll
+        for (int k = 0; k < SCAN_PER; ++k) tile[at(tid * SCAN_PER + k)] = pre + v[k];
+        const int tile_total = warp_sums[31];
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < SCAN_PER; ++k) {
+            const int i = k * SCAN_THREADS + tid;
+            if (base + i < n) a[base + i] = tile[at(i)];
+        }
+        carry += tile_total;
+        __syncthreads();  // tile and warp_sums are rewritten next round
     }
-    __syncthreads();
-    int run = x - s + (w > 0 ? warp_sums[w - 1] : 0);
-    for (int i = beg; i < end; ++i) {
-        int v = a[i];
-        a[i] = run;
-        run += v;
-    }
-    if (total && tid == 1023) *total = warp_sums[31];
+    if (total && tid == 0) *total = carry;
 }
 
 cudaError_t exclusive_scan_i32(int* data, int n, int* total, cudaStream_t s) {
