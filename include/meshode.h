@@ -119,7 +119,11 @@ size_t mo_df_noalloc_scratch_capacity(void);
 #define MO_PACKET_4x4x4 5
 #define MO_PACKET_2x4x8 6
 #define MO_PACKET_8x4x2 7
-#define MO_PACKET_LAST 7
+/* One voxel per lane, a bucket's triangles tested two at a time with packed
+ * FP32 math (for dense targets). */
+#define MO_PACKET_4x4x2_TRI2 8
+#define MO_PACKET_2x4x4_TRI2 9
+#define MO_PACKET_LAST 9
 typedef struct MoDfOptions {
     int32_t method;   /* MO_DF_AUTO, MO_DF_BRUTE or MO_DF_LBVH */
     int32_t packet;   /* MO_PACKET_* for MO_DF_LBVH */

@@ -15,6 +15,7 @@ MO_OK, MO_ERR_INVALID, MO_ERR_CUDA, MO_ERR_SCRATCH, MO_ERR_DEVICE = 0, 1, 2, 3, 
 MO_LAYOUT_LINEAR, MO_LAYOUT_CELL, MO_LAYOUT_BRICK4 = 0, 1, 2
 MO_PACKET_4x4x2, MO_PACKET_8x4x1, MO_PACKET_4x2x4, MO_PACKET_2x4x4, MO_PACKET_8x2x2 = 0, 1, 2, 3, 4
 MO_PACKET_4x4x4, MO_PACKET_2x4x8, MO_PACKET_8x4x2 = 5, 6, 7
+MO_PACKET_4x4x2_TRI2, MO_PACKET_2x4x4_TRI2 = 8, 9
 MO_DF_AUTO, MO_DF_BRUTE, MO_DF_LBVH = 0, 1, 2
 MO_EDGES_FACES, MO_EDGES_LIST = 0, 1
 MO_TILE_WARPS = 8

@@ -32,7 +32,8 @@ from ._lib import call, ptr, stream_ptr
 
 PACKETS = {"4x4x2": L.MO_PACKET_4x4x2, "8x4x1": L.MO_PACKET_8x4x1, "4x2x4": L.MO_PACKET_4x2x4,
            "2x4x4": L.MO_PACKET_2x4x4, "8x2x2": L.MO_PACKET_8x2x2,
-           "4x4x4": L.MO_PACKET_4x4x4, "2x4x8": L.MO_PACKET_2x4x8, "8x4x2": L.MO_PACKET_8x4x2}
+           "4x4x4": L.MO_PACKET_4x4x4, "2x4x8": L.MO_PACKET_2x4x8, "8x4x2": L.MO_PACKET_8x4x2,
+           "4x4x2t": L.MO_PACKET_4x4x2_TRI2, "2x4x4t": L.MO_PACKET_2x4x4_TRI2}
 LAYOUTS = {"linear": L.MO_LAYOUT_LINEAR, "cell": L.MO_LAYOUT_CELL, "brick4": L.MO_LAYOUT_BRICK4}
 TILE_WIDTHS = (4, 8)
 DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_tune", "autotune.json")

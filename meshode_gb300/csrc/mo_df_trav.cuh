@@ -163,88 +163,6 @@ __device__ __forceinline__ VoxelBand voxel_band(int x, int y, int z, int N, floa
     return b;
 }
 
-// The value the voxel (x, y, z) of this lane stores: its exact distance to
-// the nearest triangle, or `band` when that is not below the band.  All 32
-// lanes of the warp call it together and walk the tree jointly (node and
-// triangle loads are warp-uniform broadcasts); lanes with valid == false
-// only follow.  stack: this warp's TRAV_STACK ints of shared memory.
-__device__ __forceinline__ float df_voxel_value(const float4* __restrict__ nodes, const float4* __restrict__ tris,
-                                                int ntri, int N, float band, float band2, int x, int y, int z,
-                                                bool valid, int* stack, int* __restrict__ status) {
-    const int lane = threadIdx.x & 31;
-    const float Nf = (float)N;
-    const float px = __fdiv_rn((float)x, Nf), py = __fdiv_rn((float)y, Nf), pz = __fdiv_rn((float)z, Nf);
-    const VoxelBand vb = voxel_band(x, y, z, N, band, band2);
-    const float init = vb.bound2;
-    float best = valid ? init : -1.0f;
-    // Boxes are visited while their fp32 distance is within kSlack (in
-    // distance units) of the lane's best: the rounding of the box bound can
-    // exceed a triangle's computed distance by far less than that, so no
-    // triangle that could lower `best` is skipped and the result is the exact
-    // minimum of the computed distances, whatever the visit order.  Starting
-    // from band^2 instead of FLT_MAX skips what lies beyond the band and keeps
-    // every distance below it.
-    float lim = valid ? (init == FLT_MAX ? FLT_MAX : slack_bound(init)) : -1.0f;
-    const unsigned FULL = 0xffffffffu;
-    if (ntri == 1) {
-        const float t = tri_d2(px, py, pz, load_tri(tris, 0), best);
-        if (valid && t < best) best = t;
-    } else {
-        int sp = 0;
-        int node = 0;
-        // each node is entered at most once per traversal; the cap only
-        // guards against a corrupted tree
-        const int64_t max_iter = 2 * (int64_t)ntri + 64;
-        for (int64_t iter = 0;; ++iter) {
-            if (iter > max_iter) {
-                if (lane == 0) atomicOr(status, 4);
-                break;
-            }
-            const float4* nd = nodes + NODE_F4 * (int64_t)node;
-            const float4 l0 = __ldg(nd), l1 = __ldg(nd + 1), l2 = __ldg(nd + 2), l3 = __ldg(nd + 3);
-            const float4 r0 = __ldg(nd + 4), r1 = __ldg(nd + 5), r2 = __ldg(nd + 6), r3 = __ldg(nd + 7);
-            const int2 cnt = __ldg(reinterpret_cast<const int2*>(nd + 8));
-            const int L = __float_as_int(l3.w), R = __float_as_int(r3.w);
-            const int cl = cnt.x, cr = cnt.y;  // bucket sizes (0: internal)
-            const float dl = obb_d2(px, py, pz, l0, l1, l2, l3), dr = obb_d2(px, py, pz, r0, r1, r2, r3);
-            bool wl = __any_sync(FULL, dl < lim);
-            bool wr = __any_sync(FULL, dr < lim);
-            // the opened buckets' triangles, left then right, one test body
-            const int nl = wl ? cl : 0, nr = wr ? cr : 0;
-#pragma unroll 1
-            for (int k = 0; k < nl + nr; ++k) {
-                const int tri = k < nl ? ~L + k : ~R + (k - nl);
-                const float t = tri_d2(px, py, pz, load_tri(tris, tri), best);
-                if (valid && t < best) { best = t; lim = slack_bound(best); }
-            }
-            if (cl > 0) wl = false;
-            if (cr > 0) wr = false;
-            if (wl && wr) {
-                const unsigned nearer_l = __ballot_sync(FULL, valid && dl <= dr);
-                const unsigned act = __ballot_sync(FULL, valid);
-                const bool lfirst = 2 * __popc(nearer_l) >= __popc(act);
-                if (sp >= TRAV_STACK) {  // cannot happen for trees of depth <= 64
-                    if (lane == 0) atomicOr(status, 2);
-                    break;
-                }
-                if (lane == 0) stack[sp] = lfirst ? R : L;
-                ++sp;
-                node = lfirst ? L : R;
-            } else if (wl) {
-                node = L;
-            } else if (wr) {
-                node = R;
-            } else {
-                if (sp == 0) break;
-                __syncwarp();
-                node = stack[--sp];
-            }
-            __syncwarp();
-        }
-    }
-    return best < init ? __fsqrt_rn(best) : vb.value;
-}
-
 // ---------------------------------------------------------------------------
 // Two voxels per lane, on the packed FP32 pipe (FFMA2 / FADD2 / FMUL2 of
 // sm_100+): one walk of the tree serves 64 voxels, the node and triangle
@@ -321,6 +239,52 @@ __device__ __forceinline__ float2 tri_d2_2(float2 px, float2 py, float2 pz, cons
     return d;
 }
 
+// tri_d2 of one point against two triangles (both non-degenerate), each
+// element the one-triangle code's operations in its order; the cull skips
+// the rest when no lane can beat its best with either.
+__device__ __forceinline__ float2 tri_d2_t2(float px, float py, float pz, const Tri& A, const Tri& B, float cut) {
+    const float2 qx = __fadd2_rn(bc2(px), make_float2(-A.r0.x, -B.r0.x));
+    const float2 qy = __fadd2_rn(bc2(py), make_float2(-A.r0.y, -B.r0.y));
+    const float2 qz = __fadd2_rn(bc2(pz), make_float2(-A.r0.z, -B.r0.z));
+    const float2 h = __ffma2_rn(make_float2(A.r3.z, B.r3.z), qz,
+                                __ffma2_rn(make_float2(A.r3.y, B.r3.y), qy,
+                                           __fmul2_rn(make_float2(A.r3.x, B.r3.x), qx)));
+    const float2 h2 = __fmul2_rn(h, h);
+    if (!__any_sync(0xffffffffu, fminf(h2.x, h2.y) < cut)) return bc2(FLT_MAX);
+    const float2 x = __ffma2_rn(make_float2(A.r1.z, B.r1.z), qz,
+                                __ffma2_rn(make_float2(A.r1.y, B.r1.y), qy,
+                                           __fmul2_rn(make_float2(A.r1.x, B.r1.x), qx)));
+    const float2 y = __ffma2_rn(make_float2(A.r2.z, B.r2.z), qz,
+                                __ffma2_rn(make_float2(A.r2.y, B.r2.y), qy,
+                                           __fmul2_rn(make_float2(A.r2.x, B.r2.x), qx)));
+    const float2 bx = make_float2(A.r0.w, B.r0.w), cx = make_float2(A.r1.w, B.r1.w);
+    const float2 cy = make_float2(A.r2.w, B.r2.w), ebx = make_float2(A.r4.w, B.r4.w);
+    const float2 nbx = make_float2(-A.r0.w, -B.r0.w), ncx = make_float2(-A.r1.w, -B.r1.w);
+    const float2 ncy = make_float2(-A.r2.w, -B.r2.w), nebx = make_float2(-A.r4.w, -B.r4.w);
+    const float2 y2 = __fmul2_rn(y, y);
+    // A-B along the x axis
+    float2 t = clamp01_2(__fmul2_rn(x, make_float2(A.r4.x, B.r4.x)));
+    float2 dx = __ffma2_rn(t, nbx, x);
+    float2 d = __ffma2_rn(dx, dx, y2);
+    // A-C
+    t = clamp01_2(__fmul2_rn(__ffma2_rn(x, cx, __fmul2_rn(y, cy)), make_float2(A.r4.y, B.r4.y)));
+    dx = __ffma2_rn(t, ncx, x);
+    float2 dy = __ffma2_rn(t, ncy, y);
+    d = fmin2(d, __ffma2_rn(dx, dx, __fmul2_rn(dy, dy)));
+    // B-C
+    const float2 xb = __fadd2_rn(x, nbx);
+    t = clamp01_2(__fmul2_rn(__ffma2_rn(xb, ebx, __fmul2_rn(y, cy)), make_float2(A.r4.z, B.r4.z)));
+    dx = __ffma2_rn(t, nebx, xb);
+    dy = __ffma2_rn(t, ncy, y);
+    d = fmin2(d, __ffma2_rn(dx, dx, __fmul2_rn(dy, dy)));
+    const float2 sb = __ffma2_rn(ebx, y, __fmul2_rn(ncy, xb));
+    const float2 sc = __ffma2_rn(cy, x, __fmul2_rn(ncx, y));
+    const float2 hd = __fadd2_rn(h2, d);
+    const bool ina = (y.x >= 0.f) && (sb.x >= 0.f) && (sc.x >= 0.f);
+    const bool inb = (y.y >= 0.f) && (sb.y >= 0.f) && (sc.y >= 0.f);
+    return make_float2(ina ? h2.x : hd.x, inb ? h2.y : hd.y);
+}
+
 // obb_d2 for two points (a bound only: its rounding may differ from the
 // one-point form by a few ulps, far inside the traversal's slack).
 __device__ __forceinline__ float2 obb_d2_2(float2 px, float2 py, float2 pz, float4 g0, float4 g1, float4 g2,
@@ -334,6 +298,114 @@ __device__ __forceinline__ float2 obb_d2_2(float2 px, float2 py, float2 pz, floa
     const float2 s2 = make_float2(fmaxf(fmaxf(-t2.x, u2.x), 0.f), fmaxf(fmaxf(-t2.y, u2.y), 0.f));
     const float2 s3 = make_float2(fmaxf(fmaxf(-t3.x, u3.x), 0.f), fmaxf(fmaxf(-t3.y, u3.y), 0.f));
     return dot3e2(s1, s2, s3);
+}
+
+// The value the voxel (x, y, z) of this lane stores (PAIR_TRIS: a bucket's
+// triangles are tested two at a time on the packed FP32 pipe, which helps
+// dense targets and costs registers elsewhere): its exact distance to
+// the nearest triangle, or `band` when that is not below the band.  All 32
+// lanes of the warp call it together and walk the tree jointly (node and
+// triangle loads are warp-uniform broadcasts); lanes with valid == false
+// only follow.  stack: this warp's TRAV_STACK ints of shared memory.
+template <bool PAIR_TRIS = false>
+__device__ __forceinline__ float df_voxel_value(const float4* __restrict__ nodes, const float4* __restrict__ tris,
+                                                int ntri, int N, float band, float band2, int x, int y, int z,
+                                                bool valid, int* stack, int* __restrict__ status) {
+    const int lane = threadIdx.x & 31;
+    const float Nf = (float)N;
+    const float px = __fdiv_rn((float)x, Nf), py = __fdiv_rn((float)y, Nf), pz = __fdiv_rn((float)z, Nf);
+    const VoxelBand vb = voxel_band(x, y, z, N, band, band2);
+    const float init = vb.bound2;
+    float best = valid ? init : -1.0f;
+    // Boxes are visited while their fp32 distance is within kSlack (in
+    // distance units) of the lane's best: the rounding of the box bound can
+    // exceed a triangle's computed distance by far less than that, so no
+    // triangle that could lower `best` is skipped and the result is the exact
+    // minimum of the computed distances, whatever the visit order.  Starting
+    // from band^2 instead of FLT_MAX skips what lies beyond the band and keeps
+    // every distance below it.
+    float lim = valid ? (init == FLT_MAX ? FLT_MAX : slack_bound(init)) : -1.0f;
+    const unsigned FULL = 0xffffffffu;
+    if (ntri == 1) {
+        const float t = tri_d2(px, py, pz, load_tri(tris, 0), best);
+        if (valid && t < best) best = t;
+    } else {
+        int sp = 0;
+        int node = 0;
+        // each node is entered at most once per traversal; the cap only
+        // guards against a corrupted tree
+        const int64_t max_iter = 2 * (int64_t)ntri + 64;
+        for (int64_t iter = 0;; ++iter) {
+            if (iter > max_iter) {
+                if (lane == 0) atomicOr(status, 4);
+                break;
+            }
+            const float4* nd = nodes + NODE_F4 * (int64_t)node;
+            const float4 l0 = __ldg(nd), l1 = __ldg(nd + 1), l2 = __ldg(nd + 2), l3 = __ldg(nd + 3);
+            const float4 r0 = __ldg(nd + 4), r1 = __ldg(nd + 5), r2 = __ldg(nd + 6), r3 = __ldg(nd + 7);
+            const int2 cnt = __ldg(reinterpret_cast<const int2*>(nd + 8));
+            const int L = __float_as_int(l3.w), R = __float_as_int(r3.w);
+            const int cl = cnt.x, cr = cnt.y;  // bucket sizes (0: internal)
+            const float dl = obb_d2(px, py, pz, l0, l1, l2, l3), dr = obb_d2(px, py, pz, r0, r1, r2, r3);
+            bool wl = __any_sync(FULL, dl < lim);
+            bool wr = __any_sync(FULL, dr < lim);
+            // the opened buckets' triangles, left then right, one test body
+            const int nl = wl ? cl : 0, nr = wr ? cr : 0;
+            // two triangles per test where both are non-degenerate
+#pragma unroll 1
+            for (int k = 0; PAIR_TRIS && k < nl + nr; k += 2) {
+                const int ta = k < nl ? ~L + k : ~R + (k - nl);
+                const Tri A = load_tri(tris, ta);
+                if (k + 1 < nl + nr) {
+                    const int tb = k + 1 < nl ? ~L + k + 1 : ~R + (k + 1 - nl);
+                    const Tri B = load_tri(tris, tb);
+                    if (A.r3.w != 0.f && B.r3.w != 0.f) {  // warp-uniform
+                        const float2 t = tri_d2_t2(px, py, pz, A, B, best);
+                        if (valid && t.x < best) { best = t.x; lim = slack_bound(best); }
+                        if (valid && t.y < best) { best = t.y; lim = slack_bound(best); }
+                        continue;
+                    }
+                    const float t = tri_d2(px, py, pz, A, best);
+                    if (valid && t < best) { best = t; lim = slack_bound(best); }
+                    const float u = tri_d2(px, py, pz, B, best);
+                    if (valid && u < best) { best = u; lim = slack_bound(best); }
+                    continue;
+                }
+                const float t = tri_d2(px, py, pz, A, best);
+                if (valid && t < best) { best = t; lim = slack_bound(best); }
+            }
+#pragma unroll 1
+            for (int k = 0; !PAIR_TRIS && k < nl + nr; ++k) {
+                const int tri = k < nl ? ~L + k : ~R + (k - nl);
+                const float t = tri_d2(px, py, pz, load_tri(tris, tri), best);
+                if (valid && t < best) { best = t; lim = slack_bound(best); }
+            }
+            if (cl > 0) wl = false;
+            if (cr > 0) wr = false;
+            if (wl && wr) {
+                const unsigned nearer_l = __ballot_sync(FULL, valid && dl <= dr);
+                const unsigned act = __ballot_sync(FULL, valid);
+                const bool lfirst = 2 * __popc(nearer_l) >= __popc(act);
+                if (sp >= TRAV_STACK) {  // cannot happen for trees of depth <= 64
+                    if (lane == 0) atomicOr(status, 2);
+                    break;
+                }
+                if (lane == 0) stack[sp] = lfirst ? R : L;
+                ++sp;
+                node = lfirst ? L : R;
+            } else if (wl) {
+                node = L;
+            } else if (wr) {
+                node = R;
+            } else {
+                if (sp == 0) break;
+                __syncwarp();
+                node = stack[--sp];
+            }
+            __syncwarp();
+        }
+    }
+    return best < init ? __fsqrt_rn(best) : vb.value;
 }
 
 // The values of voxels (x, y, za) and (x, y, zb) of this lane, by one joint

@@ -531,7 +531,7 @@ __global__ void k_obb_nodes(const float4* __restrict__ nodes, const int2* __rest
 }
 
 // The full grid: one warp per packet of PX x PY x PZ voxels.
-template <int PX, int PY, int PZ>
+template <int PX, int PY, int PZ, bool PAIR_TRIS>
 __global__ void __launch_bounds__(TRAV_WARPS * 32) k_df_lbvh(const float4* __restrict__ nodes,
                                                              const float4* __restrict__ tris, int ntri, int N,
                                                              float band, float band2, float* __restrict__ grid,
@@ -545,7 +545,7 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) k_df_lbvh(const float4* __res
     const int ix = (int)(brick % bx), iy = (int)((brick / bx) % by), iz = (int)(brick / ((int64_t)bx * by));
     const int x = ix * PX + (lane % PX), y = iy * PY + ((lane / PX) % PY), z = iz * PZ + lane / (PX * PY);
     const bool valid = x < N && y < N && z < N;
-    const float v = df_voxel_value(nodes, tris, ntri, N, band, band2, x, y, z, valid, stack[w], status);
+    const float v = df_voxel_value<PAIR_TRIS>(nodes, tris, ntri, N, band, band2, x, y, z, valid, stack[w], status);
     if (valid) grid[((int64_t)z * N + y) * N + x] = v;
 }
 
@@ -579,12 +579,12 @@ static void launch_df_lbvh2_shape(const float4* nodes, const float4* tris, int n
     ::mo::note_launch();
 }
 
-template <int PX, int PY, int PZ>
+template <int PX, int PY, int PZ, bool PAIR_TRIS = false>
 static void launch_df_lbvh_shape(const float4* nodes, const float4* tris, int ntri, int N, float band, float band2,
                                  float* grid, int* status, cudaStream_t s) {
     const int64_t bricks = (int64_t)((N + PX - 1) / PX) * ((N + PY - 1) / PY) * ((N + PZ - 1) / PZ);
-    k_df_lbvh<PX, PY, PZ><<<ceil_div(bricks, TRAV_WARPS), TRAV_WARPS * 32, 0, s>>>(nodes, tris, ntri, N, band, band2,
-                                                                                 grid, status);
+    k_df_lbvh<PX, PY, PZ, PAIR_TRIS><<<ceil_div(bricks, TRAV_WARPS), TRAV_WARPS * 32, 0, s>>>(
+        nodes, tris, ntri, N, band, band2, grid, status);
     ::mo::note_launch();
 }
 
@@ -598,6 +598,12 @@ static void launch_df_lbvh(int packet, const float4* nodes, const float4* tris, 
         case MO_PACKET_4x4x4: launch_df_lbvh2_shape<4, 4, 2>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
         case MO_PACKET_2x4x8: launch_df_lbvh2_shape<2, 4, 4>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
         case MO_PACKET_8x4x2: launch_df_lbvh2_shape<8, 4, 1>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
+        case MO_PACKET_4x4x2_TRI2:
+            launch_df_lbvh_shape<4, 4, 2, true>(nodes, tris, ntri, N, band, band2, grid, status, s);
+            break;
+        case MO_PACKET_2x4x4_TRI2:
+            launch_df_lbvh_shape<2, 4, 4, true>(nodes, tris, ntri, N, band, band2, grid, status, s);
+            break;
         default: launch_df_lbvh_shape<4, 4, 2>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
     }
 }

@@ -78,7 +78,8 @@ def test_band_grid(cuda, name, N):
     for method, packets in ((L.MO_DF_BRUTE, [L.MO_PACKET_4x4x2]),
                             (L.MO_DF_LBVH, [L.MO_PACKET_4x4x2, L.MO_PACKET_8x4x1, L.MO_PACKET_4x2x4,
                                             L.MO_PACKET_2x4x4, L.MO_PACKET_8x2x2, L.MO_PACKET_4x4x4,
-                                            L.MO_PACKET_2x4x8, L.MO_PACKET_8x4x2])):
+                                            L.MO_PACKET_2x4x8, L.MO_PACKET_8x4x2, L.MO_PACKET_4x4x2_TRI2,
+                                            L.MO_PACKET_2x4x4_TRI2])):
         for packet in packets:
             g, _ = _build(V, F, N, method, packet, band)
             g = g.cpu().numpy()
