@@ -407,14 +407,25 @@ __device__ __forceinline__ Obb load_obb(const float4* obb, int i, float3* ns) {
 // so every lane holds the same frame).
 constexpr int OBB_WARPS = 4;
 
+// A node of at most DF_BUCKET triangles under a parent of at most DF_BUCKET
+// lies inside a bucket: the walk tests the bucket's triangles and never reads
+// its box (nor visits its parent), so none is made.
+__device__ __forceinline__ bool inside_bucket(const int2* __restrict__ range, const int* __restrict__ parent, int i) {
+    const int2 r = range[i];
+    if (i == 0 || r.y - r.x + 1 > DF_BUCKET) return false;
+    const int2 pr = range[parent[i] >> 1];
+    return pr.y - pr.x + 1 <= DF_BUCKET;
+}
+
 __global__ void __launch_bounds__(OBB_WARPS * 32) k_obb_exact(const int2* __restrict__ range, int n,
+                                                              const int* __restrict__ parent,
                                                               const float4* __restrict__ tris,
                                                               float4* __restrict__ obb) {
     const int lane = threadIdx.x & 31;
     const int i = blockIdx.x * OBB_WARPS + (threadIdx.x >> 5);
     if (i >= n - 1) return;  // warp-uniform
     const int2 r = range[i];
-    if (r.y - r.x + 1 > OBB_EXACT) return;
+    if (r.y - r.x + 1 > OBB_EXACT || inside_bucket(range, parent, i)) return;
     const unsigned FULL = 0xffffffffu;
     float3 ns = make_float3(0.f, 0.f, 0.f), v[3], nn, edge;
     for (int k = r.x + lane; k <= r.y; k += 32) {
@@ -498,10 +509,13 @@ __global__ void k_obb_walk(const float4* __restrict__ nodes, const int2* __restr
 
 // Traversal records (layout at NODE_F4 in mo_df_trav.cuh).
 __global__ void k_obb_nodes(const float4* __restrict__ nodes, const int2* __restrict__ range, int n,
-                            const float4* __restrict__ tris, const float4* __restrict__ obb,
-                            float4* __restrict__ tnodes) {
+                            const int* __restrict__ parent, const float4* __restrict__ tris,
+                            const float4* __restrict__ obb, float4* __restrict__ tnodes) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
+    // a node of at most DF_BUCKET triangles other than the root is never
+    // visited (it is its parent's bucket, or inside one)
+    if (i != 0 && range[i].y - range[i].x + 1 <= DF_BUCKET) return;
     int cnts[2];
     for (int side = 0; side < 2; ++side) {
         const int c = __float_as_int(nodes[4 * (int64_t)i + side].w);
@@ -712,12 +726,14 @@ static cudaError_t issue_tree(const BuildScratch& S, const int32_t* F, int64_t n
     if (nf > 1) {
         k_karras<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.codes_a, (int)nf, S.nodes, S.parent, S.flags, S.range);
         ::mo::note_launch();
-        k_obb_exact<<<ceil_div(nf - 1, OBB_WARPS), OBB_WARPS * 32, 0, s>>>(S.range, (int)nf, S.tris, S.obb);
+        k_obb_exact<<<ceil_div(nf - 1, OBB_WARPS), OBB_WARPS * 32, 0, s>>>(S.range, (int)nf, S.parent, S.tris,
+                                                                           S.obb);
         ::mo::note_launch();
         k_obb_walk<<<ceil_div(nf, 256), 256, 0, s>>>(S.nodes, S.range, (int)nf, S.parent, S.flags, S.tris, S.obb,
                                                      st);
         ::mo::note_launch();
-        k_obb_nodes<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.nodes, S.range, (int)nf, S.tris, S.obb, S.tnodes);
+        k_obb_nodes<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.nodes, S.range, (int)nf, S.parent, S.tris, S.obb,
+                                                          S.tnodes);
         ::mo::note_launch();
     }
     return cudaGetLastError();
