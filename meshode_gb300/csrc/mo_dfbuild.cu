@@ -467,12 +467,25 @@ __device__ void add_corners(Ext& x, float3 a1, float3 a2, float3 a3, float3 r, c
 
 // Boxes of the larger nodes, bottom-up: the second thread to reach a node
 // merges its children (normal sums; extents from the children's corners).
+// The walks start at the tree's slots (leaves and internal nodes) of at most
+// OBB_EXACT triangles whose parent holds more, so each larger node is
+// reached once from each child, and no thread climbs the levels below.
 __global__ void k_obb_walk(const float4* __restrict__ nodes, const int2* __restrict__ range, int n,
                            const int* __restrict__ parent, int* flags, const float4* __restrict__ tris,
                            float4* obb, int* status) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    int slot = (n - 1) + j;
+    if (j >= 2 * n - 1) return;
+    int slot = j;  // internal node j (j < n-1) or leaf j-(n-1)
+    {
+        const int ps = parent[slot];
+        if (ps < 0) return;  // the root
+        const int2 pr = range[ps >> 1];
+        if (pr.y - pr.x + 1 <= OBB_EXACT) return;  // the parent's box is exact
+        if (slot < n - 1) {
+            const int2 r = range[slot];
+            if (r.y - r.x + 1 > OBB_EXACT) return;  // reached by the walks below it
+        }
+    }
     for (int level = 0;; ++level) {
         if (level > 128) {
             atomicOr(status, 4);
@@ -729,7 +742,8 @@ static cudaError_t issue_tree(const BuildScratch& S, const int32_t* F, int64_t n
         k_obb_exact<<<ceil_div(nf - 1, OBB_WARPS), OBB_WARPS * 32, 0, s>>>(S.range, (int)nf, S.parent, S.tris,
                                                                            S.obb);
         ::mo::note_launch();
-        k_obb_walk<<<ceil_div(nf, 256), 256, 0, s>>>(S.nodes, S.range, (int)nf, S.parent, S.flags, S.tris, S.obb,
+        k_obb_walk<<<ceil_div(2 * nf - 1, 256), 256, 0, s>>>(S.nodes, S.range, (int)nf, S.parent, S.flags, S.tris,
+                                                             S.obb,
                                                      st);
         ::mo::note_launch();
         k_obb_nodes<<<ceil_div(nf - 1, 256), 256, 0, s>>>(S.nodes, S.range, (int)nf, S.parent, S.tris, S.obb,
