@@ -7,6 +7,8 @@
 // key = 2*h + role, role 0 when the vertex is the half-edge's v0 (the
 // reference's `g[v0] -= r`), 1 when it is v1 (`g[v1] += r`).  Rows are sorted
 // by key, i.e. in the order the reference's serial loop touches the vertex.
+#include <climits>
+
 #include "mo_common.cuh"
 
 namespace mo {
@@ -103,13 +105,50 @@ __global__ void k_csr_fill(const int32_t* __restrict__ idx, int64_t nh, int kind
     other[p1] = v0;
 }
 
-// Rows are short (vertex degree); insertion sort by key makes the order
-// independent of the atomic fill order.
+// Rows are short (vertex degree); sorting each by key makes the order
+// independent of the atomic fill order.  Keys are distinct (2h for the v0
+// role of half-edge h, 2h+1 for v1, also when v0 == v1), so any sort gives
+// the same row: rows of up to 16 go through a bitonic network in registers,
+// longer ones an insertion sort in place.
+constexpr int ROW_NET = 16;
+
 __global__ void k_csr_sort_rows(int64_t nv, const int* __restrict__ row_ptr, int* __restrict__ key,
                                 int* __restrict__ other) {
     const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nv) return;
     const int b = row_ptr[v], e = row_ptr[v + 1];
+    if (e - b <= ROW_NET) {
+        const int len = e - b;
+        int k[ROW_NET], o[ROW_NET];
+#pragma unroll
+        for (int i = 0; i < ROW_NET; ++i) {
+            k[i] = i < len ? key[b + i] : INT_MAX;  // padding sorts last
+            o[i] = i < len ? other[b + i] : 0;
+        }
+#pragma unroll
+        for (int w = 2; w <= ROW_NET; w <<= 1)
+#pragma unroll
+            for (int j = w >> 1; j > 0; j >>= 1)
+#pragma unroll
+                for (int i = 0; i < ROW_NET; ++i) {
+                    const int l = i ^ j;
+                    if (l > i) {
+                        const bool up = (i & w) == 0;
+                        if ((k[i] > k[l]) == up) {
+                            const int tk = k[i], to = o[i];
+                            k[i] = k[l]; o[i] = o[l];
+                            k[l] = tk; o[l] = to;
+                        }
+                    }
+                }
+#pragma unroll
+        for (int i = 0; i < ROW_NET; ++i)
+            if (i < len) {
+                key[b + i] = k[i];
+                other[b + i] = o[i];
+            }
+        return;
+    }
     for (int i = b + 1; i < e; ++i) {
         const int k = key[i], o = other[i];
         int j = i - 1;
