@@ -57,7 +57,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--requests", type=int, default=512)
     ap.add_argument("--req-steps", type=int, default=500)
-    ap.add_argument("--group-steps", type=int, default=25)
+    ap.add_argument("--group-steps", type=int, default=10)
     ap.add_argument("--plain-sample", type=int, default=6)
     ap.add_argument("--cpu-sample-s", type=float, default=20.0)
     ap.add_argument("--no-extras", action="store_true", help="skip latency/plain/cpu legs")
@@ -66,7 +66,7 @@ def parse():
     ap.add_argument("--df-mode", default="full", choices=["on-demand", "full"],
                     help="grids filled cell by cell as vertices reach them, or built whole at admission")
     ap.add_argument("--build-streams", type=int, default=6)
-    ap.add_argument("--max-building", type=int, default=16)
+    ap.add_argument("--max-building", type=int, default=32)
     ap.add_argument("--engine", default="native", choices=["native", "python"],
                     help="serving loop: the C++ pool behind mo_pool_* or the Python engine")
     return ap.parse_args()
