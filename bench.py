@@ -471,16 +471,31 @@ def ode_config():
     torch.cuda.synchronize()
     plain = e0.elapsed_time(e1) / 3
     plain_mem = torch.cuda.max_memory_allocated() - base
+    # the same fit keeping every stage's activations (no recompute)
+    dfm.store_activations = True
+    dfm.step()
+    torch.cuda.synchronize()
+    base = torch.cuda.memory_allocated()
+    torch.cuda.reset_peak_memory_stats()
+    e0.record()
+    for _ in range(3):
+        dfm.step()
+    e1.record()
+    torch.cuda.synchronize()
+    stored = e0.elapsed_time(e1) / 3
+    stored_mem = torch.cuda.max_memory_allocated() - base
     n = dfm.x0.shape[0]
     eval_flops = 2 * n * (3 * 256 + 2 * 256 * 256 + 256 * 3)
     # 80 evaluations forward, 80 recomputed and 80 back-propagated (~2x) in the adjoint
     flops = eval_flops * (80 + 80 + 2 * 80)
     return {"source_vertices": n, "hidden": 256, "rk4_steps": 20, "N": 128,
             "ms_per_iteration": ours, "peak_extra_mem_gb": ours_mem / 1e9,
+            "stored_activations_ms_per_iteration": stored, "stored_activations_peak_extra_mem_gb": stored_mem / 1e9,
             "torch_autograd_ms_per_iteration": plain, "torch_autograd_peak_extra_mem_gb": plain_mem / 1e9,
             "tflops": flops / (ours * 1e-3) / 1e12,
             "note": "checkpointed adjoint: recomputes each RK4 step's activations (4/3 of the FLOPs) to hold "
-                    "one step's activations instead of all 80 stage evaluations'"}
+                    "one step's activations instead of all 80 stage evaluations'; stored_activations: the same "
+                    "fit keeping them (same gradients bit for bit)"}
 
 
 # ---------------------------------------------------------------------------

@@ -14,7 +14,9 @@ the graph/DF losses, back-propagating through the stored RK4 graph.  Here:
 * the backward pass is a checkpointed adjoint: only the state at the start
   of every RK4 step is kept; each step's four stage activations are
   recomputed and back-propagated in reverse, accumulating the parameter
-  gradients.
+  gradients (``store_activations=True`` keeps every stage's activations
+  from the forward instead: plain autograd's memory, no recompute, the same
+  gradients bit for bit).
 
 The m x m layers are cuBLAS fp32 GEMMs (TF32 must be off:
 ``torch.backends.cuda.matmul.allow_tf32 = False``, torch's default); the
@@ -111,20 +113,26 @@ def _vjp(params, grads, st, g_out):
 
 
 class ODEFlow(Function):
-    """x(1) = RK4^steps(x(0)) under the velocity MLP, with a checkpointed
-    adjoint backward (states at step starts kept, stage activations
-    recomputed)."""
+    """x(1) = RK4^steps(x(0)) under the velocity MLP, with an adjoint
+    backward.  store=False: checkpointed (states at step starts kept, each
+    step's stage activations recomputed in the backward: one step's
+    activations in memory); store=True: every stage's activations kept from
+    the forward (the memory of plain autograd, no recompute).  Both give the
+    same gradients bit for bit (the recompute repeats the same kernels)."""
 
     @staticmethod
-    def forward(ctx, x0, steps, W1, b1, W2, b2, W3, b3, W4, b4):
+    def forward(ctx, x0, steps, store, W1, b1, W2, b2, W3, b3, W4, b4):
         params = [t.detach().contiguous() for t in (W1, b1, W2, b2, W3, b3, W4, b4)]
         steps = int(steps)
         h = 1.0 / steps
         x = x0.detach().contiguous()
         ckpt = torch.empty(steps, x.shape[0], 3, dtype=torch.float32, device=x.device)
+        ctx.stages = [] if store else None
         for k in range(steps):
             ckpt[k].copy_(x)
-            x, _ = _rk4_step(params, x, h, store=False)
+            x, st = _rk4_step(params, x, h, store=bool(store))
+            if store:
+                ctx.stages.append(st)
         ctx.save_for_backward(ckpt, *params)
         ctx.steps = steps
         return x
@@ -137,7 +145,11 @@ class ODEFlow(Function):
         grads = [torch.zeros_like(p) for p in params]
         a = a_out.contiguous().float()
         for k in reversed(range(steps)):
-            _, st = _rk4_step(params, ckpt[k], h, store=True)
+            if ctx.stages is not None:
+                st = ctx.stages[k]
+                ctx.stages[k] = None  # freed as the backward passes it
+            else:
+                _, st = _rk4_step(params, ckpt[k], h, store=True)
             dk4 = a * (h / 6)
             g4 = _vjp(params, grads, st[3], dk4)
             dx = a + g4
@@ -148,7 +160,8 @@ class ODEFlow(Function):
             g1 = _vjp(params, grads, st[0], a * (h / 6) + (h / 2) * g2)
             dx += g1
             a = dx
-        return (a, None) + tuple(grads)
+        ctx.stages = None
+        return (a, None, None) + tuple(grads)
 
 
 class FitLossFunction(Function):
@@ -176,7 +189,7 @@ class NeuralODEDeformer:
     MLP parameters are the optimisation variables (torch.optim.Adam)."""
 
     def __init__(self, src_V, src_F, tar_V, tar_F, grid_resolution=128, rigidity=0.1, hidden=256, steps=20,
-                 seed=4, lr=1e-3):
+                 seed=4, lr=1e-3, store_activations=False):
         L.require_cuda()
         if torch.backends.cuda.matmul.allow_tf32:
             raise RuntimeError("TF32 matmul is enabled; the ODE fit needs fp32 GEMMs "
@@ -189,11 +202,13 @@ class NeuralODEDeformer:
         PD.StoreRigidityInformation(self.x0, self.F, self.pid)
         self.rigidity2 = float(torch.tensor(rigidity * rigidity, dtype=torch.float32))
         self.steps = int(steps)
+        # False: checkpointed adjoint (low memory); True: activations kept (faster)
+        self.store_activations = bool(store_activations)
         self.params = [p.requires_grad_(True) for p in init_params(hidden, seed, dev)]
         self.opt = torch.optim.Adam(self.params, lr=lr)
 
     def deformed(self):
-        return ODEFlow.apply(self.x0, self.steps, *self.params)
+        return ODEFlow.apply(self.x0, self.steps, self.store_activations, *self.params)
 
     def loss(self):
         return FitLossFunction.apply(self.deformed(), self.F, self.pid, self.rigidity2)

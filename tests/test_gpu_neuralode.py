@@ -122,3 +122,24 @@ def test_fit_decreases_loss(problem):
     for _ in range(30):
         l1 = float(dfm.step())
     assert l1 < l0
+
+
+def test_stored_activations_give_the_same_gradients(cuda):
+    """store_activations=True skips the adjoint's recompute; the gradients
+    and the updated parameters are the checkpointed mode's, bit for bit."""
+    rng = np.random.Generator(np.random.PCG64(9))
+    Vs, Fs = meshgen.icosphere(3)
+    Vt, Ft = meshgen.icosphere(4)
+    Vt = meshgen.displace(Vt, rng)
+    args = (torch.from_numpy((Vs * 0.8).astype(np.float32)), torch.from_numpy(Fs.astype(np.int32)),
+            torch.from_numpy(Vt.astype(np.float32)), torch.from_numpy(Ft.astype(np.int32)))
+    runs = []
+    for store in (False, True):
+        d = neuralode.NeuralODEDeformer(*args, grid_resolution=32, rigidity=0.1, hidden=64, steps=5, seed=4,
+                                        store_activations=store)
+        losses = [d.step() for _ in range(3)]
+        runs.append((losses, [p.detach().clone() for p in d.params]))
+    (la, pa), (lb, pb) = runs
+    assert all(torch.equal(x, y) for x, y in zip(la, lb))
+    assert all(torch.equal(x, y) for x, y in zip(pa, pb))
+
