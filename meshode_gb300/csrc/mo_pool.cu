@@ -529,15 +529,19 @@ int run_group(MoPool* P) {
         PCHK(cudaMemcpyAsync(denorm, normed, 12 * nv, cudaMemcpyDeviceToDevice, P->step));
         rc = mo_normalize(denorm, nv, R->params, 1, sv);
         if (rc) return rc;
-        const cudaMemcpyKind ok = R->in.out_on_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
-        if (R->in.V_out) PCHK(cudaMemcpyAsync(R->in.V_out, denorm, 12 * nv, ok, P->step));
-        if (R->in.V_normalized_out)
-            PCHK(cudaMemcpyAsync(R->in.V_normalized_out, normed, 12 * nv, cudaMemcpyDeviceToDevice, P->step));
+        // the loss (its buffer is rewritten by the next group) and the DF
+        // status (on-demand fills report traversal faults there) on the step
+        // stream; the result copies on the io stream, off the steps' path
         PCHK(cudaMemcpyAsync(&R->host->loss, P->pair_loss + (int64_t)(k - 1) * n + i, 8, cudaMemcpyDeviceToHost,
                              P->step));
-        // DF status again: on-demand fills report traversal faults there
         PCHK(cudaMemcpyAsync(R->host->status, R->status, 16, cudaMemcpyDeviceToHost, P->step));
         PCHK(cudaEventRecord(R->ev, P->step));
+        PCHK(cudaStreamWaitEvent(P->io, R->ev, 0));
+        const cudaMemcpyKind ok = R->in.out_on_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+        if (R->in.V_out) PCHK(cudaMemcpyAsync(R->in.V_out, denorm, 12 * nv, ok, P->io));
+        if (R->in.V_normalized_out)
+            PCHK(cudaMemcpyAsync(R->in.V_normalized_out, normed, 12 * nv, cudaMemcpyDeviceToDevice, P->io));
+        PCHK(cudaEventRecord(R->ev, P->io));  // DONE when both streams' copies are
         free_state(R, P->step);
         R->phase = 4;
         P->retiring.push_back(id);

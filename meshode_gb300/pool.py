@@ -104,7 +104,7 @@ class NativePool:
         # result buffers the pool fills as the request retires
         nv = int(tensors[0].shape[0])
         if self.results_to_host:
-            out = torch.empty(nv, 3, dtype=torch.float32).pin_memory()
+            out = torch.empty(nv, 3, dtype=torch.float32, pin_memory=True)
         else:
             out = torch.empty(nv, 3, dtype=torch.float32, device=self.device)
         normed = torch.empty(nv, 3, dtype=torch.float32, device=self.device)
