@@ -626,12 +626,19 @@ def ours_arm(args, world, rank):
         return
     extras = {}
     if not args.no_extras:
-        # latency under Poisson arrivals at 200 requests/s
-        lat_reqs = fresh(req_dev)
-        engine.run(lat_reqs, realtime=True)
-        lats = np.asarray([r.latency for r in lat_reqs]) * 1e3
-        extras["latency_ms"] = {"p50": float(np.percentile(lats, 50)), "p95": float(np.percentile(lats, 95)),
-                                "p99": float(np.percentile(lats, 99)), "arrivals": "poisson 200 req/s"}
+        # latency under Poisson arrivals at 200 requests/s: three runs, the
+        # median one (by p99) reported, every run's p99 listed (a single run
+        # can catch a host stall of tens of ms)
+        runs = []
+        for _ in range(3):
+            lat_reqs = fresh(req_dev)
+            engine.run(lat_reqs, realtime=True)
+            lats = np.asarray([r.latency for r in lat_reqs]) * 1e3
+            runs.append([float(np.percentile(lats, q)) for q in (50, 95, 99)])
+        runs.sort(key=lambda x: x[2])
+        p50, p95, p99 = runs[1]
+        extras["latency_ms"] = {"p50": p50, "p95": p95, "p99": p99, "arrivals": "poisson 200 req/s",
+                                "runs_p99": [r[2] for r in runs], "reported": "median of 3 runs by p99"}
         extras["saturated_latency_ms_p99"] = float(np.percentile(
             np.asarray([r.latency for r in last]) * 1e3, 99))
         if args.engine == "native" and df_mode == L.MO_DF_ON_DEMAND:
