@@ -9,6 +9,7 @@ and collects finished ones.  A request's result is bit-identical to the
 Python engine's and to the request run alone.
 """
 import ctypes
+import gc
 import time
 
 import torch
@@ -164,8 +165,21 @@ class NativePool:
         # pool's own streams read them
         torch.cuda.current_stream(self.device).synchronize()
         total = len(requests)
-        ndone = 0
         nfin = ctypes.c_int64()
+        # the garbage collector is held off while the loop serves: a full
+        # collection over the requests' objects stalls it for tens of ms
+        gc_on = gc.isenabled()
+        gc.disable()
+        try:
+            wall = self._serve(future, total, realtime, nfin)
+        finally:
+            if gc_on:
+                gc.enable()
+        self._accumulate_groups()
+        return wall
+
+    def _serve(self, future, total, realtime, nfin):
+        ndone = 0
         i = 0
         t0 = time.perf_counter()
         while ndone < total:
@@ -189,9 +203,7 @@ class NativePool:
             check(self.lib.mo_pool_progress(self._h, 1, ctypes.byref(nfin)), "mo_pool_progress")
             ndone += self._collect()
         torch.cuda.synchronize(self.device)
-        wall = time.perf_counter() - t0
-        self._accumulate_groups()
-        return wall
+        return time.perf_counter() - t0
 
     def _accumulate_groups(self):
         ms, nb = ctypes.c_double(), ctypes.c_double()
