@@ -25,6 +25,7 @@ same, bit for bit, whether the request ran alone or in any mix.
 """
 import collections
 import ctypes
+import gc
 import time
 
 import numpy as np
@@ -238,7 +239,18 @@ class ServingEngine:
     def run(self, requests, realtime=False, measure_groups=True):
         """Serve ``requests`` to completion.  With realtime=True a request
         becomes visible at its ``arrival`` time (seconds after the start);
-        otherwise all are queued at the start.  Returns the wall time (s)."""
+        otherwise all are queued at the start.  Returns the wall time (s).
+        The garbage collector is held off while serving (a full collection
+        stalls the loop for tens of ms)."""
+        gc_on = gc.isenabled()
+        gc.disable()
+        try:
+            return self._serve(requests, realtime, measure_groups)
+        finally:
+            if gc_on:
+                gc.enable()
+
+    def _serve(self, requests, realtime, measure_groups):
         lib = L.lib()
         future = collections.deque(sorted(requests, key=lambda r: r.arrival))
         pending = collections.deque()
