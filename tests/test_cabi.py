@@ -115,3 +115,28 @@ def test_pool_argument_errors_without_gpu():
     assert lib.mo_pool_submit(None, ctypes.byref(req), ctypes.byref(nid)) == L.MO_ERR_INVALID
     assert lib.mo_pool_progress(None, 0, None) == L.MO_ERR_INVALID
     assert lib.mo_pool_destroy(None) == L.MO_OK
+    cfg = L.MoPoolConfig(max_pairs=4, max_tiles=10, group_steps=5, df_mode=7)
+    assert lib.mo_pool_create(ctypes.byref(cfg), ctypes.byref(out)) == L.MO_ERR_INVALID
+    assert b"df_mode" in lib.mo_last_error()
+    assert lib.mo_pool_fill_totals(None, None) == L.MO_ERR_INVALID
+
+
+def test_distance_field_entry_points_check_arguments_without_gpu():
+    """The tree-only build, the on-demand fills and the packet shapes are
+    checked on the host before anything runs."""
+    B.build()
+    lib = L.lib()
+    assert lib.mo_df_tree_bytes(0) == 0
+    assert lib.mo_df_tree_bytes(3) == 16 * (5 * 3 + 9 * 2)
+    assert lib.mo_df_tree_scratch_bytes(-1, 3) == 0
+    assert lib.mo_df_tree_build(None, 10, None, 4, None, None, 0, None, None, None) == L.MO_ERR_INVALID
+    assert b"null" in lib.mo_last_error()
+    assert lib.mo_df_lazy_bytes(1) == 0 and lib.mo_df_lazy_bytes(L.MO_DF_LAZY_MAX_N + 1) == 0
+    assert lib.mo_df_lazy_seed(None, 0, None, -1, None, None, None, 0, None) == L.MO_ERR_INVALID
+    assert lib.mo_df_lazy_seed(None, 0, None, 0, None, None, None, 0, None) == L.MO_OK  # nothing to seed
+    assert lib.mo_df_lazy_fill(None, None, None, None, -1, None, None) == L.MO_ERR_INVALID
+    assert lib.mo_df_lazy_fill(None, None, None, None, 1 << 28, None, None) == L.MO_ERR_INVALID
+    opt = L.MoDfOptions(L.MO_DF_LBVH, L.MO_PACKET_2x4x4_TRI2 + 1, 0.0)
+    rc = lib.mo_df_build_ex(None, 10, None, 4, 64, None, ctypes.byref(opt), None, 0, None, None, None)
+    assert rc == L.MO_ERR_INVALID and b"packet" in lib.mo_last_error()
+    assert lib.mo_fused_step_on_demand(None, None, None, 4, 0, None, 0, None) == L.MO_ERR_INVALID
