@@ -96,13 +96,19 @@ int mo_lbvh_build(const float* V, int64_t nv, const int32_t* F, int64_t nf, cons
  * fixed device array of MO_DF_NOALLOC_SCRATCH_BYTES that every GPU loading
  * this library holds until the process exits; targets whose scratch need
  * (mo_df_build_scratch_bytes with mo_df_method_for's method) exceeds it are
- * rejected with MO_ERR_SCRATCH -- about 50,000 triangles.  The caller still
- * passes the inputs and the output grid.  The first call on a device, made
- * with that device current, looks up the array's device address; make that
- * first call before any stream capture.  Every call shares the array and
- * leaves its contents behind: calls that overlap on the GPU (other streams,
- * other host threads) race and must be serialised by the caller.  The call
- * synchronises `stream` to read the build status. */
+ * rejected with MO_ERR_SCRATCH.  The LBVH build needs about 427 bytes per
+ * triangle plus 12 per vertex, so the array holds targets of up to 19,000
+ * triangles with up to 10,000 vertices (a closed mesh has about half as
+ * many vertices as triangles).  The caller still passes the inputs and the
+ * output grid.  The first call on a device, made with that device current,
+ * looks up the array's device address (under lazy module loading that may
+ * also be when the array is placed in device memory) and caches it: make one
+ * warm-up call per device at start-up, before the phase that must not
+ * allocate, and do not use the library across a cudaDeviceReset.  The call
+ * cannot be made during stream capture: it copies the build status to the
+ * host and synchronises `stream`.  Every call shares the array and leaves
+ * its contents behind: calls that overlap on the GPU (other streams, other
+ * host threads) race and must be serialised by the caller. */
 #define MO_DF_NOALLOC_SCRATCH_BYTES (8u << 20)
 int mo_df_build_noalloc(const float* V, int64_t nv, const int32_t* F, int64_t nf, int N,
                         const double* params4, float* grid_linear_out, void* stream);
@@ -176,7 +182,7 @@ int mo_grid_relayout(const float* grid_linear, int N, int layout, float* out, vo
 /* ------------------------------------------------------------------------
  * DistanceFieldLoss.  Replaces DistanceFieldLoss_forward
  * (src/interface/distance_layer.cc:8-37, per vertex d(v)^2 with
- * UniformGrid::DistanceFloat, src/lib/uniformgrid.cc:120-185) and
+ * UniformGrid::DistanceFloat, src/lib/uniformgrid.cc:85-150) and
  * DistanceFieldLoss_backward (distance_layer.cc:39-81, d * grad d through
  * ceres::Jet<float,3>).  Bit-identical to the reference's float arithmetic.
  * ------------------------------------------------------------------------ */

@@ -1,5 +1,5 @@
 // Trilinear distance lookup with its forward-mode derivative, bit-identical to
-// UniformGrid::DistanceFloat<ceres::Jet<float,3>> (src/lib/uniformgrid.cc:120-185)
+// UniformGrid::DistanceFloat<ceres::Jet<float,3>> (src/lib/uniformgrid.cc:85-150)
 // as evaluated by the reference for DistanceFieldLoss (distance_layer.cc:58-78).
 //
 // The jet arithmetic is specialised by hand: the seed derivatives of p are unit
@@ -63,7 +63,7 @@ __device__ __forceinline__ DFJet df_eval(const float* __restrict__ grid, int N, 
     const float sx = MUL(x, Nf), sy = MUL(y, Nf), sz = MUL(z, Nf);
     const int px = trunc_i32_x86(sx), py = trunc_i32_x86(sy), pz = trunc_i32_x86(sz);
     if (px < 0 || py < 0 || pz < 0 || px >= N - 1 || py >= N - 1 || pz >= N - 1) {
-        // Out-of-box linear penalty (uniformgrid.cc:125-150): no cutoff here,
+        // Out-of-box linear penalty (uniformgrid.cc:90-115): no cutoff here,
         // and no term for an axis with p == N-1.
         float l = 0.0f, gx = 0.0f, gy = 0.0f, gz = 0.0f;
         if (px < 0) { l = ADD(l, -sx); gx = -Nf; }
@@ -98,7 +98,7 @@ __device__ __forceinline__ DFJet df_eval(const float* __restrict__ grid, int N, 
             rz = (k == 0) ? Wz : ADD(rz, Wz);
         }
     }
-    if (ra > 0.2f) {  // uniformgrid.cc:182-183
+    if (ra > 0.2f) {  // uniformgrid.cc:147-148
         r.d = 0.0f; r.gx = 0.0f; r.gy = 0.0f; r.gz = 0.0f;
     } else {
         r.d = ra; r.gx = rx; r.gy = ry; r.gz = rz;

@@ -993,8 +993,9 @@ std::mutex g_noalloc_mu;
 void* g_noalloc_addr[kMaxDevices] = {};
 }  // namespace
 
-// Device address of the fixed scratch on the current device (looked up on the
-// first call made with that device current).
+// Device address of the fixed scratch on the current device, looked up on the
+// first call made with that device current and cached for the process: the
+// cached address is not valid across a cudaDeviceReset of that device.
 static int noalloc_scratch_address(void** out) {
     int dev = 0;
     MO_CUDA(cudaGetDevice(&dev));

@@ -3,7 +3,7 @@
 // The reference builds the whole grid before the optimisation loop
 // (Mesh::ConstructDistanceField, src/lib/mesh.cc:106-152) and every step reads
 // the eight corners of the cell each vertex lies in (UniformGrid::
-// DistanceFloat, src/lib/uniformgrid.cc:120-185).  Over a whole fit the
+// DistanceFloat, src/lib/uniformgrid.cc:85-150).  Over a whole fit the
 // vertices visit a small part of the grid, so here a cell's corners are
 // computed the first time a vertex reaches the cell:
 //   * admission: the target's traversal tree (mo_df_tree_build), and the

@@ -38,7 +38,7 @@
 
 /* ------------------------------------------------------------------------ */
 /* Float -> int truncation with x86-64 semantics.                           */
-/* uniformgrid.cc:122-124 does `int px = *(float*)&p[0] * grid_dimension_`. */
+/* uniformgrid.cc:87-89 does `int px = *(float*)&p[0] * grid_dimension_`. */
 /* On x86-64 (cvttss2si) NaN and out-of-range values give INT_MIN.          */
 /* ------------------------------------------------------------------------ */
 static int trunc_i32(float f) {
@@ -49,7 +49,7 @@ static int trunc_i32(float f) {
 EXPORT int orc_trunc_i32(float f) { return trunc_i32(f); }
 
 /* ------------------------------------------------------------------------ */
-/* UniformGrid::DistanceFloat<float>  (src/lib/uniformgrid.cc:120-150)       */
+/* UniformGrid::DistanceFloat<float>  (src/lib/uniformgrid.cc:85-150)       */
 /* Grid storage is voxel_distance_[z][y][x] (uniformgrid.h:33), flattened    */
 /* here to grid[(z*N + y)*N + x], values already cast to float.              */
 /* ------------------------------------------------------------------------ */
@@ -116,7 +116,7 @@ static inline jet3 jmul(jet3 f, jet3 g) {
     return r;
 }
 
-/* UniformGrid::DistanceFloat<ceres::Jet<float,3>> (uniformgrid.cc:120-185),
+/* UniformGrid::DistanceFloat<ceres::Jet<float,3>> (uniformgrid.cc:85-150),
  * written against the jet operations exactly as the template expands.
  * out[0] = value, out[1..3] = d value / d p. */
 EXPORT void orc_distance_jet(const float* grid, int N, const float* pv, float* out) {

@@ -6,7 +6,7 @@ arithmetic, written here in numpy scalar float32 operations (one rounding per
 operation, no fused multiply-add) and numpy float64:
 
 * UniformGrid::DistanceFloat<float> and <ceres::Jet<float,3>>
-  (src/lib/uniformgrid.cc:120-185) -- a small dual-number class;
+  (src/lib/uniformgrid.cc:85-150) -- a small dual-number class;
 * DistanceFieldLoss_forward/_backward (src/interface/distance_layer.cc:8-81);
 * StoreRigidityInformation / RigidEdgeLoss_forward / _backward
   (src/interface/rigid_layer.cc:11-133), serial loops;

@@ -1,7 +1,7 @@
 """The bound behind the distance-field band of the two lowest layers (CPU).
 
 A lookup with a coordinate in (-1/N, 0) extrapolates from cell 0 of that
-axis (UniformGrid::DistanceFloat, uniformgrid.cc:120-185: the cell index
+axis (UniformGrid::DistanceFloat, uniformgrid.cc:85-150: the cell index
 truncates toward zero and the weight is the coordinate times N).  With corner
 values 1/N apart differing by at most h = 1/N (distances and their clamps are
 1-Lipschitz), the extrapolated trilinear value is at least the smallest

@@ -140,3 +140,21 @@ def test_distance_field_entry_points_check_arguments_without_gpu():
     rc = lib.mo_df_build_ex(None, 10, None, 4, 64, None, ctypes.byref(opt), None, 0, None, None, None)
     assert rc == L.MO_ERR_INVALID and b"packet" in lib.mo_last_error()
     assert lib.mo_fused_step_on_demand(None, None, None, 4, 0, None, 0, None) == L.MO_ERR_INVALID
+
+
+def test_noalloc_capacity_matches_documented_figure():
+    """The header documents that mo_df_build_noalloc's fixed array holds
+    targets of up to 19,000 triangles with up to 10,000 vertices; the
+    library's own scratch planner must agree, so the figure cannot drift."""
+    B.build()
+    lib = L.lib()
+    cap = lib.mo_df_noalloc_scratch_capacity()
+    src = open(HEADER).read()
+    assert "19,000" in src and "10,000 vertices" in src
+    assert lib.mo_df_method_for(19_000, 64) == L.MO_DF_LBVH
+    for N in (32, 64, 128, 256):
+        m = lib.mo_df_method_for(19_000, N)
+        assert lib.mo_df_build_scratch_bytes(10_000, 19_000, N, m) <= cap
+        # about 5% more triangles no longer fit
+        m = lib.mo_df_method_for(20_000, N)
+        assert lib.mo_df_build_scratch_bytes(10_000, 20_000, N, m) > cap

@@ -5,7 +5,7 @@ mo_df_loss_band) on the GPU.
   other voxel holds the band; in the two lowest layers along each axis the
   band is band + 13/N.  The same for both methods and every packet shape.
 * DistanceFieldLoss forward and backward (UniformGrid::DistanceFloat through
-  the jet, uniformgrid.cc:120-185) from the banded grid equal, bit for bit,
+  the jet, uniformgrid.cc:85-150) from the banded grid equal, bit for bit,
   those from the exact grid at points everywhere: inside the cube, near the
   surface, on the 0.2 cutoff, in the extrapolation slab (-1/N, 0) of each
   axis, in the penalty region; in every grid layout.

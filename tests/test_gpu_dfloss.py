@@ -1,7 +1,7 @@
 """DistanceFieldLoss forward/backward on the GPU against the oracle, bit for bit.
 
 Reference: src/interface/distance_layer.cc:8-81 with
-UniformGrid::DistanceFloat (src/lib/uniformgrid.cc:120-185).  The GPU grid is
+UniformGrid::DistanceFloat (src/lib/uniformgrid.cc:85-150).  The GPU grid is
 handed to the oracle so the comparison isolates the lookup and its jet
 derivative; both must agree exactly (integer-equal bit patterns).
 """

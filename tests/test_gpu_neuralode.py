@@ -3,7 +3,7 @@ against an FP64 reference.
 
 The FP64 reference is the same model written with torch float64 autograd on
 the CPU: the MLP, 20 classic RK4 steps, the distance lookup restated from
-UniformGrid::distance<double> (src/lib/uniformgrid.cc:53-118: truncation
+UniformGrid::distance<double> (src/lib/uniformgrid.cc:18-83: truncation
 toward zero, the out-of-box penalty without the N-1 slab, the 0.2 cutoff) on
 the GPU grid, and the rigidity term with the fp32 rest offsets.  It is
 itself checked against FP64 central differences (h = 1e-6).  The GPU fp32

@@ -3,7 +3,7 @@
 * point-triangle distance in the vertex, edge and face regions and for
   degenerate triangles;
 * the trilinear lookup reproduces a linear field, and every branch of
-  UniformGrid::DistanceFloat (src/lib/uniformgrid.cc:120-185): below zero,
+  UniformGrid::DistanceFloat (src/lib/uniformgrid.cc:85-150): below zero,
   beyond N, the N-1 slab without a term, truncation toward zero, the 0.2
   cutoff;
 * the jet derivative agrees with FP64 finite differences (h = 1e-6) of an FP64

@@ -8,9 +8,13 @@ inside libmeshode.so instead of caller or library allocations.
 Two calls in a row through the C ABI, on two different targets (the second
 takes the other build method, so it runs over what the first left in the
 shared array), each compared with the regular entry point mo_df_build given
-caller scratch, within the distance-field tolerance of the other GPU tests
-(1e-5 of the normalised target's bounding-box diagonal).  A target too large
-for the fixed array is refused with MO_ERR_SCRATCH.
+caller scratch.  Both take the same method and kernels on the same input, so
+the grids must be equal bit for bit: a stale value left in the shared array
+would show up here even if it moved a distance by one ulp.  Each grid is
+also compared once with the FP64 oracle, within the distance-field tolerance
+of the other GPU tests (1e-5 of the normalised target's bounding-box
+diagonal).  A target too large for the fixed array is refused with
+MO_ERR_SCRATCH.
 
 The file is named so that pytest collects it last.
 """
@@ -20,6 +24,7 @@ import torch
 
 from meshode_gb300 import _lib as L
 from meshode_gb300 import meshgen
+from oracle import pydeform_oracle as orc
 
 pytestmark = pytest.mark.gpu
 
@@ -79,7 +84,11 @@ def test_noalloc_matches_regular_build_twice(cuda):
         ref = _regular(V, F, N, prm)
         torch.cuda.synchronize()
         assert torch.isfinite(grid).all()
-        err = (grid.double() - ref.double()).abs().max().item()
+        assert torch.equal(grid, ref)
+        p = prm.cpu().numpy()
+        Vn = orc.normalized_double(V.cpu().numpy(), float(p[0]), p[1:])
+        exact = orc.df_build(Vn, F.cpu().numpy(), N)
+        err = np.abs(grid.cpu().numpy().astype(np.float64) - exact).max()
         assert err <= TOL_REL_DIAG * _diag(V, prm), err
 
 
