@@ -428,7 +428,10 @@ static double btree_query(const btree* t, const double* p, double best) {
     stack[sp++] = 0;
     while (sp) {
         const bnode* nd = &t->nodes[stack[--sp]];
-        if (box_dist2(p, nd->lo, nd->hi) >= best) continue;
+        /* prune with a relative margin far above the rounding of box_dist2
+         * and orc_point_tri_dist2, so the result is the exact minimum of the
+         * computed distances over every triangle (what brute force returns) */
+        if (box_dist2(p, nd->lo, nd->hi) > best * (1.0 + 1e-9)) continue;
         if (nd->left < 0) {
             for (int i = nd->start; i < nd->start + nd->count; ++i) {
                 int f = t->order[i];
@@ -446,6 +449,72 @@ static double btree_query(const btree* t, const double* p, double best) {
         }
     }
     return best;
+}
+
+/* Nearest triangle of every point of P through the AABB tree: the squared
+ * distance and the face index (the lowest index among exact ties found first
+ * in the tree's order).  The libigl stand-in of oracle/_ref calls this in
+ * place of igl::point_mesh_squared_distance; C (np x 3) is filled with NaN.
+ * nthreads <= 0 uses every OpenMP thread.  Returns 0 on success. */
+static double btree_query_idx(const btree* t, const double* p, int* best_f) {
+    double best = DBL_MAX;
+    int bf = -1;
+    int stack[128]; int sp = 0;
+    stack[sp++] = 0;
+    while (sp) {
+        const bnode* nd = &t->nodes[stack[--sp]];
+        if (box_dist2(p, nd->lo, nd->hi) > best * (1.0 + 1e-9)) continue;  /* as btree_query */
+        if (nd->left < 0) {
+            for (int i = nd->start; i < nd->start + nd->count; ++i) {
+                int f = t->order[i];
+                double d = orc_point_tri_dist2(p, t->V + 3 * (int64_t)t->F[3 * (int64_t)f],
+                                               t->V + 3 * (int64_t)t->F[3 * (int64_t)f + 1],
+                                               t->V + 3 * (int64_t)t->F[3 * (int64_t)f + 2]);
+                if (d < best || (d == best && f < bf)) { best = d; bf = f; }
+            }
+        } else {
+            const bnode* L = &t->nodes[nd->left];
+            const bnode* R = &t->nodes[nd->right];
+            double dl = box_dist2(p, L->lo, L->hi), dr = box_dist2(p, R->lo, R->hi);
+            if (dl < dr) { stack[sp++] = nd->right; stack[sp++] = nd->left; }
+            else { stack[sp++] = nd->left; stack[sp++] = nd->right; }
+        }
+    }
+    *best_f = bf;
+    return best;
+}
+
+EXPORT int orc_point_mesh_sqdist(const double* P, int64_t np, const double* V, int64_t nv, const int* F,
+                                 int64_t nf, double* sqrD, int* I, double* C, int nthreads) {
+    (void)nthreads;
+    if (nf <= 0 || nv <= 0) return -1;
+    for (int64_t k = 0; k < 3 * nf; ++k)
+        if (F[k] < 0 || F[k] >= nv) return -3;
+    btree t;
+    t.V = V; t.F = F; t.nn = 0;
+    t.order = (int*)malloc(sizeof(int) * (size_t)nf);
+    t.cen = (double*)malloc(sizeof(double) * 3 * (size_t)nf);
+    t.nodes = (bnode*)malloc(sizeof(bnode) * 2 * (size_t)nf);
+    if (!t.order || !t.cen || !t.nodes) { free(t.order); free(t.cen); free(t.nodes); return -2; }
+    for (int64_t f = 0; f < nf; ++f) {
+        t.order[f] = (int)f;
+        for (int c = 0; c < 3; ++c)
+            t.cen[3 * f + c] = (V[3 * (int64_t)F[3 * f] + c] + V[3 * (int64_t)F[3 * f + 1] + c] +
+                                V[3 * (int64_t)F[3 * f + 2] + c]) / 3.0;
+    }
+    btree_build(&t, 0, (int)nf);
+#ifdef _OPENMP
+    int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nt)
+#endif
+    for (int64_t q = 0; q < np; ++q) {
+        int f;
+        sqrD[q] = btree_query_idx(&t, P + 3 * q, &f);
+        I[q] = f;
+        for (int c = 0; c < 3; ++c) C[3 * q + c] = NAN;
+    }
+    free(t.order); free(t.cen); free(t.nodes);
+    return 0;
 }
 
 /* DF through the AABB tree over a list of voxels (all when vox == NULL).
