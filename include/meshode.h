@@ -226,6 +226,25 @@ int mo_edge_csr_build(const int32_t* idx, int64_t n_items, int kind, int64_t nv,
 int mo_edge_backward(const float* V, int64_t nv, const void* csr, int64_t nh, const float* off,
                      float* grad_out, void* stream);
 
+/* Weighted edges.  Replaces StoreCadInformation / CadEdgeLoss_forward /
+ * CadEdgeLoss_backward (src/interface/cad_layer.cc:11-223).  The CAD loss's
+ * edge set is E's edges followed by F's half-edges: list_out [ne+3nf, 2]
+ * (cad_layer.cc:33-67).  Its rest offsets come from mo_edge_offsets over that
+ * list (MO_EDGES_LIST), its weights lambda_out [H] =
+ * 2e-2 / (|off| + 1e-8) (cad_layer.cc:48-49, 71-72: the float norm, then
+ * double, rounded to float). */
+int mo_edge_cad_list(const int32_t* E, int64_t ne, const int32_t* F, int64_t nf, int32_t* list_out,
+                     void* stream);
+int mo_edge_cad_weights(const float* off, int64_t nh, float* lambda_out, void* stream);
+/* mo_edge_forward / mo_edge_backward with a per-edge weight w [H] (NULL: the
+ * unweighted calls): loss_out [H,3] = ((v1 - v0 - off) * w)^2 per component
+ * (cad_layer.cc:114-122); grad_out [nv,3] = the serial scatter of
+ * (v1 - v0 - off) * (w * w) (cad_layer.cc:195-202). */
+int mo_edge_forward_w(const float* V, int64_t nv, const int32_t* idx, int64_t n_items, int kind,
+                      const float* off, const float* w, float* loss_out, void* stream);
+int mo_edge_backward_w(const float* V, int64_t nv, const void* csr, int64_t nh, const float* off,
+                       const float* w, float* grad_out, void* stream);
+
 /* Sliced-ELL (32-vertex slices, column-major records) view of the CSR for
  * the fused step: one int32 record per incident half-edge, other | role<<31
  * (role 1 when the vertex is the half-edge's v1), in half-edge order;

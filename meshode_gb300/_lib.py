@@ -110,6 +110,10 @@ _SIGS = {
     "mo_edge_csr_bytes": (_SZ, [_I64, _I64, _I]),
     "mo_edge_csr_build": (_I, [_P, _I64, _I, _I64, _P, _SZ, _P, _P]),
     "mo_edge_backward": (_I, [_P, _I64, _P, _I64, _P, _P, _P]),
+    "mo_edge_cad_list": (_I, [_P, _I64, _P, _I64, _P, _P]),
+    "mo_edge_cad_weights": (_I, [_P, _I64, _P, _P]),
+    "mo_edge_forward_w": (_I, [_P, _I64, _P, _I64, _I, _P, _P, _P, _P]),
+    "mo_edge_backward_w": (_I, [_P, _I64, _P, _I64, _P, _P, _P, _P]),
     "mo_sell_plan": (_I, [_P, _I64, _I64, _P, _P]),
     "mo_sell_fill": (_I, [_P, _I64, _I64, _P, _P, _P]),
     "mo_adam_step": (_I, [_P, _P, _P, _P, _I64, _F, _F, _F, _F, _F, _F, _P]),

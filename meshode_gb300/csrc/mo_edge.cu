@@ -192,6 +192,91 @@ __global__ void __launch_bounds__(256) k_edge_backward(const float* __restrict__
     G[3 * i] = gx; G[3 * i + 1] = gy; G[3 * i + 2] = gz;
 }
 
+// ---------------------------------------------------------------------------
+// Weighted edges (CadEdgeLoss, src/interface/cad_layer.cc:11-223).
+//
+// The CAD loss's edge set is E's edges followed by F's half-edges
+// (cad_layer.cc:33-67, 108-143, 178-219), one rest offset and one weight
+// lambda_e = 2e-2 / (|off_e| + 1e-8) each (:48-49, :71-72).  The forward is
+// ((v1 - v0 - off) * lambda)^2 per component (:114-122); the backward
+// scatters (v1 - v0 - off) * (lambda * lambda) (:195-202) in the same serial
+// order as the unweighted loss.
+// ---------------------------------------------------------------------------
+__global__ void k_edge_cad_list(const int32_t* __restrict__ E, int64_t ne, const int32_t* __restrict__ F,
+                                int64_t nf, int32_t* __restrict__ out) {
+    const int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= ne + 3 * nf) return;
+    int v0, v1;
+    if (h < ne) {
+        v0 = E[2 * h];
+        v1 = E[2 * h + 1];
+    } else {
+        he_ends(F, MO_EDGES_FACES, h - ne, v0, v1);
+    }
+    out[2 * h] = v0;
+    out[2 * h + 1] = v1;
+}
+
+// |off| is Eigen's float norm: sqrt of x*x + (y*y + z*z) (its unrolled
+// pairwise sum of three terms); the +1e-8 and the quotient are double (the
+// literals are double), rounded to float on the store.
+__global__ void k_edge_cad_weights(const float* __restrict__ off, int64_t nh, float* __restrict__ lam) {
+    const int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= nh) return;
+    const float x = off[3 * h], y = off[3 * h + 1], z = off[3 * h + 2];
+    const float n = __fsqrt_rn(ADD(MUL(x, x), ADD(MUL(y, y), MUL(z, z))));
+    lam[h] = __double2float_rn(__ddiv_rn(2e-2, __dadd_rn((double)n, 1e-8)));
+}
+
+__global__ void k_edge_forward_w(const float* __restrict__ V, int64_t nv, const int32_t* __restrict__ idx,
+                                 int64_t nh, int kind, const float* __restrict__ off, const float* __restrict__ w,
+                                 float* __restrict__ L) {
+    const int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= nh) return;
+    int v0, v1;
+    he_ends(idx, kind, h, v0, v1);
+    if (!in_range(v0, nv) || !in_range(v1, nv)) {
+        L[3 * h] = L[3 * h + 1] = L[3 * h + 2] = __int_as_float(0x7fc00000);
+        return;
+    }
+    const float lam = w[h];
+    for (int c = 0; c < 3; ++c) {
+        const float r = MUL(SUB(SUB(V[3 * (int64_t)v1 + c], V[3 * (int64_t)v0 + c]), off[3 * h + c]), lam);
+        L[3 * h + c] = MUL(r, r);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_edge_backward_w(const float* __restrict__ V, int64_t nv,
+                                                         const int* __restrict__ row_ptr,
+                                                         const int* __restrict__ key,
+                                                         const int* __restrict__ other,
+                                                         const float* __restrict__ off,
+                                                         const float* __restrict__ w, float* __restrict__ G) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    const float px = V[3 * i], py = V[3 * i + 1], pz = V[3 * i + 2];
+    float gx = 0.0f, gy = 0.0f, gz = 0.0f;
+    const int b = row_ptr[i], e = row_ptr[i + 1];
+    for (int k = b; k < e; ++k) {
+        const int kk = key[k];
+        const int64_t h = kk >> 1;
+        const int64_t o = other[k];
+        const float qx = V[3 * o], qy = V[3 * o + 1], qz = V[3 * o + 2];
+        const float ox = off[3 * h], oy = off[3 * h + 1], oz = off[3 * h + 2];
+        const float l2 = MUL(w[h], w[h]);
+        if ((kk & 1) == 0) {  // v0: g[v0] -= (v1 - v0 - off) * lambda^2
+            gx = SUB(gx, MUL(SUB(SUB(qx, px), ox), l2));
+            gy = SUB(gy, MUL(SUB(SUB(qy, py), oy), l2));
+            gz = SUB(gz, MUL(SUB(SUB(qz, pz), oz), l2));
+        } else {              // v1: g[v1] += (v1 - v0 - off) * lambda^2
+            gx = ADD(gx, MUL(SUB(SUB(px, qx), ox), l2));
+            gy = ADD(gy, MUL(SUB(SUB(py, qy), oy), l2));
+            gz = ADD(gz, MUL(SUB(SUB(pz, qz), oz), l2));
+        }
+    }
+    G[3 * i] = gx; G[3 * i + 1] = gy; G[3 * i + 2] = gz;
+}
+
 // Slice widths (max row length over 32 consecutive vertices), x32.
 __global__ void k_sell_width(int64_t nv, int64_t nslices, const int* __restrict__ row_ptr,
                              int* __restrict__ slice_ptr) {
@@ -321,6 +406,53 @@ extern "C" int mo_edge_backward(const float* V, int64_t nv, const void* csr, int
     k_edge_backward<<<ceil_div(nv, 256), 256, 0, as_stream(stream)>>>(V, nv, c.row_ptr, c.key, c.other, off,
                                                                       grad_out); ::mo::note_launch();
     MO_LAUNCH_CHECK("k_edge_backward");
+    return MO_OK;
+}
+
+extern "C" int mo_edge_cad_list(const int32_t* E, int64_t ne, const int32_t* F, int64_t nf, int32_t* list_out,
+                                void* stream) {
+    MO_CHECK_ARG(ne >= 0 && nf >= 0, "negative size");
+    const int64_t nh = ne + 3 * nf;
+    MO_CHECK_ARG(nh < ((int64_t)1 << 30), "too many edges (%lld)", (long long)nh);
+    if (nh == 0) return MO_OK;
+    MO_CHECK_ARG((ne == 0 || E) && (nf == 0 || F) && list_out, "null pointer");
+    k_edge_cad_list<<<ceil_div(nh, 256), 256, 0, as_stream(stream)>>>(E, ne, F, nf, list_out); ::mo::note_launch();
+    MO_LAUNCH_CHECK("k_edge_cad_list");
+    return MO_OK;
+}
+
+extern "C" int mo_edge_cad_weights(const float* off, int64_t nh, float* lambda_out, void* stream) {
+    MO_CHECK_ARG(nh >= 0 && nh < ((int64_t)1 << 30), "bad edge count (%lld)", (long long)nh);
+    if (nh == 0) return MO_OK;
+    MO_CHECK_ARG(off && lambda_out, "null pointer");
+    k_edge_cad_weights<<<ceil_div(nh, 256), 256, 0, as_stream(stream)>>>(off, nh, lambda_out); ::mo::note_launch();
+    MO_LAUNCH_CHECK("k_edge_cad_weights");
+    return MO_OK;
+}
+
+extern "C" int mo_edge_forward_w(const float* V, int64_t nv, const int32_t* idx, int64_t n_items, int kind,
+                                 const float* off, const float* w, float* loss_out, void* stream) {
+    if (!w) return mo_edge_forward(V, nv, idx, n_items, kind, off, loss_out, stream);
+    int64_t nh;
+    int rc = check_edges(V, nv, idx, n_items, kind, &nh);
+    if (rc) return rc;
+    if (nh == 0) return MO_OK;
+    MO_CHECK_ARG(off && loss_out, "null offset or output pointer");
+    k_edge_forward_w<<<ceil_div(nh, 256), 256, 0, as_stream(stream)>>>(V, nv, idx, nh, kind, off, w, loss_out); ::mo::note_launch();
+    MO_LAUNCH_CHECK("k_edge_forward_w");
+    return MO_OK;
+}
+
+extern "C" int mo_edge_backward_w(const float* V, int64_t nv, const void* csr, int64_t nh, const float* off,
+                                  const float* w, float* grad_out, void* stream) {
+    if (!w) return mo_edge_backward(V, nv, csr, nh, off, grad_out, stream);
+    MO_CHECK_ARG(nv >= 0 && nh >= 0, "negative size");
+    if (nv == 0) return MO_OK;
+    MO_CHECK_ARG(V && csr && grad_out && (nh == 0 || off), "null pointer");
+    CsrView c = csr_view(const_cast<void*>(csr), nv, nh);
+    k_edge_backward_w<<<ceil_div(nv, 256), 256, 0, as_stream(stream)>>>(V, nv, c.row_ptr, c.key, c.other, off, w,
+                                                                        grad_out); ::mo::note_launch();
+    MO_LAUNCH_CHECK("k_edge_backward_w");
     return MO_OK;
 }
 

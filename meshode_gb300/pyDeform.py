@@ -14,9 +14,9 @@ all additive:
 * Template handles are ints into a process-global list, as in
   deform_params.cc:7-14; ``ReleaseTemplate`` frees one's device memory.
 
-Not provided here (outside the deformation hot path): ``LoadCadMesh`` (CGAL
-remeshing), ``SolveLinear`` (Eigen sparse solve) and the unused
-``CadEdgeLoss`` family; they raise NotImplementedError.
+``LoadCadMesh`` (the reference's CGAL remeshing) is restated on the CPU in
+``cadmesh``; ``SolveLinear`` runs in libmeshode.so (matrix-free conjugate
+gradients in double).
 """
 import ctypes
 
@@ -39,6 +39,7 @@ class _EdgeState:
         self.csr_cache = {}         # key -> (idx_dev, csr buffer)
         self.csr = None             # CSR of the index tensor given at Store time
         self.rest = None            # the vertices the rest offsets were taken from
+        self.weights = None         # float32 [nh] per-edge weights (CadEdgeLoss)
 
 
 class DeformParams:
@@ -190,11 +191,83 @@ def SolveLinear(tensorV, tensorF, tensorE, tensorRef, tensorGraphV, rigidity, wi
     return it.value, res.value
 
 
-def StoreCadInformation(*args, **kwargs):
-    raise NotImplementedError("CadEdgeLoss has no working caller in the reference and is not provided")
+def _cad_edges(state, tensorF, tensorE, nv, dev):
+    """(device edge list, validated CSR) of the CAD loss's edge set -- E's
+    edges then F's half-edges (cad_layer.cc:33-67) -- cached by the identity
+    and version of F and E."""
+    key = ("cad", _idx_key(tensorF, nv), _idx_key(tensorE, nv))
+    hit = state.csr_cache.get(key)
+    if hit is not None:
+        return hit
+    Fd = _on_device(tensorF, dev)
+    Ed = _on_device(tensorE, dev)
+    nh = Ed.shape[0] + 3 * Fd.shape[0]
+    lst = torch.empty(nh, 2, dtype=torch.int32, device=dev)
+    call("mo_edge_cad_list", ptr(Ed), Ed.shape[0], ptr(Fd), Fd.shape[0], ptr(lst), stream_ptr())
+    nbytes = L.lib().mo_edge_csr_bytes(nv, nh, L.MO_EDGES_LIST)
+    csr = torch.empty((nbytes + 3) // 4, dtype=torch.int32, device=dev)
+    call("mo_edge_csr_build", ptr(lst), nh, L.MO_EDGES_LIST, nv, ptr(csr), nbytes, None, stream_ptr())
+    if len(state.csr_cache) > 8:
+        state.csr_cache.clear()
+    state.csr_cache[key] = (lst, csr)
+    return state.csr_cache[key]
 
 
-CadEdgeLoss_forward = CadEdgeLoss_backward = StoreCadInformation
+def StoreCadInformation(tensorV, tensorF, tensorE, param_id):
+    """Rest offsets and weights 2e-2/(|off|+1e-8) of E's edges then F's
+    half-edges (cad_layer.cc:11-77)."""
+    _check_vertices(tensorV)
+    _check_indices(tensorF, 3, "F")
+    _check_indices(tensorE, 2, "E")
+    p = GetParams(param_id)
+    Vd = _on_device(tensorV, p.device)
+    nh = tensorE.shape[0] + 3 * tensorF.shape[0]
+    off = torch.empty(nh, 3, dtype=torch.float32, device=p.device)
+    state = _EdgeState(L.MO_EDGES_LIST, None, nh, off)
+    lst, state.csr = _cad_edges(state, tensorF, tensorE, Vd.shape[0], p.device)
+    state.idx = lst
+    s = stream_ptr()
+    call("mo_edge_offsets", ptr(Vd), Vd.shape[0], ptr(lst), nh, L.MO_EDGES_LIST, ptr(off), s)
+    state.weights = torch.empty(nh, dtype=torch.float32, device=p.device)
+    call("mo_edge_cad_weights", ptr(off), nh, ptr(state.weights), s)
+    state.rest = Vd.clone()
+    p.edge = state
+
+
+def _cad_state(param_id, tensorV, tensorF, tensorE):
+    _check_vertices(tensorV)
+    _check_indices(tensorF, 3, "F")
+    _check_indices(tensorE, 2, "E")
+    p = GetParams(param_id)
+    st = p.edge
+    if st is None or st.weights is None:
+        raise RuntimeError("template %d has no CAD edge information; call StoreCadInformation first"
+                           % int(param_id))
+    nh = tensorE.shape[0] + 3 * tensorF.shape[0]
+    if nh != st.nh:
+        raise RuntimeError("edge set has %d edges but the stored rest offsets have %d" % (nh, st.nh))
+    Vd = _on_device(tensorV, p.device)
+    lst, csr = _cad_edges(st, tensorF, tensorE, Vd.shape[0], p.device)
+    return p, st, Vd, lst, csr
+
+
+def CadEdgeLoss_forward(tensorV, tensorF, tensorE, param_id):
+    """[E+3F,3] weighted squared residual components (cad_layer.cc:79-150)."""
+    p, st, Vd, lst, _ = _cad_state(param_id, tensorV, tensorF, tensorE)
+    out = torch.empty(st.nh, 3, dtype=torch.float32, device=p.device)
+    call("mo_edge_forward_w", ptr(Vd), Vd.shape[0], ptr(lst), st.nh, L.MO_EDGES_LIST, ptr(st.offsets),
+         ptr(st.weights), ptr(out), stream_ptr())
+    return _out(out, tensorV)
+
+
+def CadEdgeLoss_backward(tensorV, tensorF, tensorE, param_id):
+    """[V,3] scatter of the residuals times the squared weights
+    (cad_layer.cc:152-223)."""
+    p, st, Vd, _, csr = _cad_state(param_id, tensorV, tensorF, tensorE)
+    out = torch.empty(Vd.shape[0], 3, dtype=torch.float32, device=p.device)
+    call("mo_edge_backward_w", ptr(Vd), Vd.shape[0], ptr(csr), st.nh, ptr(st.offsets), ptr(st.weights), ptr(out),
+         stream_ptr())
+    return _out(out, tensorV)
 
 
 # ---------------------------------------------------------------------------
@@ -361,7 +434,7 @@ def _csr_for(state, idx, idx_dev, nv, dev):
 def _edge_state(param_id, kind, idx):
     p = GetParams(param_id)
     st = p.edge
-    if st is None or st.kind != kind:
+    if st is None or st.kind != kind or st.weights is not None:
         raise RuntimeError("template %d has no %s information; call %s first" % (
             int(param_id), "rigidity" if kind == L.MO_EDGES_FACES else "graph",
             "StoreRigidityInformation" if kind == L.MO_EDGES_FACES else "StoreGraphInformation"))

@@ -241,6 +241,53 @@ EXPORT void orc_edge_backward(const float* V, int64_t nv, const int* idx, int64_
     }
 }
 
+/* StoreCadInformation (cad_layer.cc:11-77): the CAD loss's edge set is E's
+ * edges, then F's half-edges (list [ne + 3nf][2]); each edge's weight is
+ * lambda = 2e-2 / (|off| + 1e-8) with |off| Eigen's float norm (sqrt of
+ * x*x + (y*y + z*z)) and the sum and quotient in double (:48-49, :71-72). */
+EXPORT void orc_edge_cad_list(const int* E, int64_t ne, const int* F, int64_t nf, int* list) {
+    for (int64_t h = 0; h < ne; ++h) { list[2 * h] = E[2 * h]; list[2 * h + 1] = E[2 * h + 1]; }
+    for (int64_t h = 0; h < 3 * nf; ++h) {
+        int v0, v1; he_ends(F, 0, h, &v0, &v1);
+        list[2 * (ne + h)] = v0; list[2 * (ne + h) + 1] = v1;
+    }
+}
+
+EXPORT void orc_edge_cad_weights(const float* off, int64_t nh, float* lam) {
+    for (int64_t h = 0; h < nh; ++h) {
+        float x = off[3 * h], y = off[3 * h + 1], z = off[3 * h + 2];
+        float n = sqrtf(x * x + (y * y + z * z));
+        lam[h] = (float)(2e-2 / ((double)n + 1e-8));
+    }
+}
+
+/* CadEdgeLoss_forward (cad_layer.cc:108-143): ((v1 - v0 - off) * w)^2. */
+EXPORT void orc_edge_forward_w(const float* V, const int* idx, int64_t nh, int kind,
+                               const float* off, const float* w, float* L) {
+    for (int64_t h = 0; h < nh; ++h) {
+        int v0, v1; he_ends(idx, kind, h, &v0, &v1);
+        for (int c = 0; c < 3; ++c) {
+            float r = (V[3 * (int64_t)v1 + c] - V[3 * (int64_t)v0 + c] - off[3 * h + c]) * w[h];
+            L[3 * h + c] = r * r;
+        }
+    }
+}
+
+/* CadEdgeLoss_backward (cad_layer.cc:178-219): serial scatter of
+ * (v1 - v0 - off) * (w * w). */
+EXPORT void orc_edge_backward_w(const float* V, int64_t nv, const int* idx, int64_t nh, int kind,
+                                const float* off, const float* w, float* Gout) {
+    memset(Gout, 0, sizeof(float) * 3 * (size_t)nv);
+    for (int64_t h = 0; h < nh; ++h) {
+        int v0, v1; he_ends(idx, kind, h, &v0, &v1);
+        float l2 = w[h] * w[h];
+        for (int c = 0; c < 3; ++c) {
+            Gout[3 * (int64_t)v0 + c] -= (V[3 * (int64_t)v1 + c] - V[3 * (int64_t)v0 + c] - off[3 * h + c]) * l2;
+            Gout[3 * (int64_t)v1 + c] += (V[3 * (int64_t)v1 + c] - V[3 * (int64_t)v0 + c] - off[3 * h + c]) * l2;
+        }
+    }
+}
+
 /* ------------------------------------------------------------------------ */
 /* Normalisation.                                                            */
 /* Mesh::Normalize (src/lib/mesh.cc:66-96) on float input promoted to double, */

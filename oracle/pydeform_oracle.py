@@ -36,6 +36,10 @@ def lib():
         L.orc_edge_offsets.argtypes = [P, P, i64, ctypes.c_int, P]
         L.orc_edge_forward.argtypes = [P, P, i64, ctypes.c_int, P, P]
         L.orc_edge_backward.argtypes = [P, i64, P, i64, ctypes.c_int, P, P]
+        L.orc_edge_cad_list.argtypes = [P, i64, P, i64, P]
+        L.orc_edge_cad_weights.argtypes = [P, i64, P]
+        L.orc_edge_forward_w.argtypes = [P, P, i64, ctypes.c_int, P, P, P]
+        L.orc_edge_backward_w.argtypes = [P, i64, P, i64, ctypes.c_int, P, P, P]
         L.orc_normalize_params.argtypes = [P, i64, P, P]
         L.orc_normalize_double.argtypes = [P, i64, ctypes.c_double, P, P]
         L.orc_normalize_by_template.argtypes = [P, i64, ctypes.c_double, P]
@@ -168,6 +172,37 @@ def edge_backward(V, idx, kind, off):
     nh = edge_count(idx, kind)
     Gd = np.empty((V.shape[0], 3), np.float32)
     lib().orc_edge_backward(_p(V), V.shape[0], _p(idx), nh, kind, _p(off), _p(Gd))
+    return Gd
+
+
+def cad_edge_list(F, E):
+    """E's edges then F's half-edges, the CAD loss's edge set (cad_layer.cc:33-67)."""
+    F = _i32(F); E = _i32(E)
+    out = np.empty((E.shape[0] + 3 * F.shape[0], 2), np.int32)
+    lib().orc_edge_cad_list(_p(E), E.shape[0], _p(F), F.shape[0], _p(out))
+    return out
+
+
+def cad_edge_weights(off):
+    off = _f32(off)
+    lam = np.empty(off.shape[0], np.float32)
+    lib().orc_edge_cad_weights(_p(off), off.shape[0], _p(lam))
+    return lam
+
+
+def edge_forward_w(V, idx, kind, off, w):
+    V = _f32(V); idx = _i32(idx); off = _f32(off); w = _f32(w)
+    nh = edge_count(idx, kind)
+    L = np.empty((nh, 3), np.float32)
+    lib().orc_edge_forward_w(_p(V), _p(idx), nh, kind, _p(off), _p(w), _p(L))
+    return L
+
+
+def edge_backward_w(V, idx, kind, off, w):
+    V = _f32(V); idx = _i32(idx); off = _f32(off); w = _f32(w)
+    nh = edge_count(idx, kind)
+    Gd = np.empty((V.shape[0], 3), np.float32)
+    lib().orc_edge_backward_w(_p(V), V.shape[0], _p(idx), nh, kind, _p(off), _p(w), _p(Gd))
     return Gd
 
 
@@ -305,6 +340,25 @@ def StoreRigidityInformation(V, F, pid):
 
 def StoreGraphInformation(V, E, pid):
     _params[pid].edge_offset = edge_offsets(V, E, 1)
+
+
+def StoreCadInformation(V, F, E, pid):
+    """cad_layer.cc:11-77: rest offsets and weights of E's edges then F's
+    half-edges."""
+    lst = cad_edge_list(F, E)
+    p = _params[pid]
+    p.edge_offset = edge_offsets(V, lst, 1)
+    p.edge_lambda = cad_edge_weights(p.edge_offset)
+
+
+def CadEdgeLoss_forward(V, F, E, pid):
+    p = _params[pid]
+    return torch.from_numpy(edge_forward_w(V, cad_edge_list(F, E), 1, p.edge_offset, p.edge_lambda))
+
+
+def CadEdgeLoss_backward(V, F, E, pid):
+    p = _params[pid]
+    return torch.from_numpy(edge_backward_w(V, cad_edge_list(F, E), 1, p.edge_offset, p.edge_lambda))
 
 
 def DistanceFieldLoss_forward(V, pid):

@@ -109,3 +109,38 @@ def test_empty_edges(cuda):
     assert out.shape == (0, 3)
     g = PD.RigidEdgeLoss_backward(torch.from_numpy(V0).to(cuda), torch.from_numpy(F).to(cuda), pid)
     assert torch.all(g == 0)
+
+
+@pytest.mark.parametrize("level", [1, 3])
+def test_cad_edges_bitexact(cuda, orc, level):
+    """StoreCadInformation / CadEdgeLoss_forward/_backward
+    (src/interface/cad_layer.cc:11-223): E's edges then F's half-edges with
+    weights 2e-2/(|off|+1e-8); forward ((r*w)^2), backward (serial scatter of
+    r*w^2) bit for bit against the oracle, from CPU and CUDA tensors, with
+    duplicated and degenerate (v0 == v1, zero offset) edges in E."""
+    rng = np.random.Generator(np.random.PCG64(10 + level))
+    V, F = meshgen.icosphere(level)
+    V0 = (V * 0.3 + 0.5).astype(np.float32)
+    F = F.astype(np.int32)
+    E = meshgen.edges_from_faces(F)[::2]
+    E = np.concatenate([E, E[:5], np.array([[0, 0], [1, 1]], np.int32)]).astype(np.int32)
+    pid = _template(cuda)
+    Vt, Ft, Et = torch.from_numpy(V0), torch.from_numpy(F), torch.from_numpy(E)
+    PD.StoreCadInformation(Vt, Ft, Et, pid)
+    opid = orc.InitializeDeformTemplate(np.zeros((3, 3), np.float32), np.array([[0, 1, 2]], np.int32), 0, 2,
+                                        grid=np.zeros(8, np.float32))
+    orc.StoreCadInformation(V0, F, E, opid)
+    st = PD.GetParams(pid).edge
+    assert _same(st.offsets.cpu().numpy(), orc.GetParams(opid).edge_offset)[0]
+    assert _same(st.weights.cpu().numpy(), orc.GetParams(opid).edge_lambda)[0]
+    V1 = (V0 + rng.normal(scale=0.01, size=V0.shape)).astype(np.float32)
+    for dev in ("cpu", cuda):
+        Vx = torch.from_numpy(V1).to(dev)
+        f = PD.CadEdgeLoss_forward(Vx, Ft.to(dev), Et.to(dev), pid).cpu().numpy()
+        b = PD.CadEdgeLoss_backward(Vx, Ft.to(dev), Et.to(dev), pid).cpu().numpy()
+        ok, n = _same(f, orc.CadEdgeLoss_forward(V1, F, E, opid).numpy())
+        assert ok, n
+        ok, n = _same(b, orc.CadEdgeLoss_backward(V1, F, E, opid).numpy())
+        assert ok, n
+    with pytest.raises(RuntimeError):
+        PD.RigidEdgeLoss_forward(torch.from_numpy(V1), Ft, pid)  # the template holds CAD edges now

@@ -41,8 +41,11 @@ def test_validation_errors_without_gpu():
         PD.InitializeDeformTemplate(torch.zeros(5, 3), torch.zeros(2, 3, dtype=torch.int32), 0, 1)
     with pytest.raises(FileNotFoundError):
         PD.LoadCadMesh("x.obj")
-    with pytest.raises(NotImplementedError):
+    with pytest.raises(RuntimeError):
         PD.StoreCadInformation(None, None, None, 0)
+    with pytest.raises(RuntimeError):
+        PD.CadEdgeLoss_forward(torch.zeros(5, 3), torch.zeros(2, 3, dtype=torch.int32),
+                               torch.zeros(1, 3, dtype=torch.int32), 0)
 
 
 def test_generators():

@@ -242,3 +242,28 @@ def test_rigid_loop_matches_reference_layers(orc, meshes):
     orc.StoreRigidityInformation(Vo, SF, opid)
     out, _ = orc.rigid_fit(Vo, SF, opid, 20)
     assert _bits_equal(src_V.detach().numpy(), out.numpy())
+
+
+def test_cad_edges(orc, meshes):
+    """StoreCadInformation / CadEdgeLoss_forward/_backward
+    (cad_layer.cc:11-223): E's edges then F's half-edges, the weights
+    2e-2/(|off|+1e-8), the weighted residuals and their serial scatter, on
+    the CAD source with its unique edges as E."""
+    V, F = meshes["cad-source.obj"]
+    Fn = F.numpy()
+    E = np.unique(np.sort(np.concatenate([Fn[:, [0, 1]], Fn[:, [1, 2]]]), axis=1), axis=0)
+    E = torch.from_numpy(np.ascontiguousarray(E[::3].astype(np.int32)))
+    pid = R.grid_template(np.zeros(8), 2)
+    opid = orc.InitializeDeformTemplate(np.zeros((3, 3), np.float32), np.array([[0, 1, 2]], np.int32), 0, 2,
+                                        grid=np.zeros(8, np.float32))
+    R.StoreCadInformation(V, F, E, pid)
+    orc.StoreCadInformation(V, F, E, opid)
+    nh = E.shape[0] + 3 * F.shape[0]
+    off, lam = R.template_edges(pid, nh)
+    assert _bits_equal(off, orc.GetParams(opid).edge_offset)
+    assert _bits_equal(lam, orc.GetParams(opid).edge_lambda)
+    rng = np.random.Generator(np.random.PCG64(9))
+    W = (V + torch.from_numpy(rng.normal(0, 0.02, V.shape).astype(np.float32))).contiguous()
+    assert _bits_equal(R.CadEdgeLoss_forward(W, F, E, pid).numpy(), orc.CadEdgeLoss_forward(W, F, E, opid).numpy())
+    assert _bits_equal(R.CadEdgeLoss_backward(W, F, E, pid).numpy(),
+                       orc.CadEdgeLoss_backward(W, F, E, opid).numpy())
