@@ -144,6 +144,16 @@ typedef struct MoDfOptions {
 int mo_df_build_ex(const float* V, int64_t nv, const int32_t* F, int64_t nf, int N,
                    const double* params4, const MoDfOptions* opt, void* scratch, size_t scratch_bytes,
                    float* grid_linear_out, int32_t* status_out, void* stream);
+/* mo_df_build_ex that also measures the work of the nearest-triangle search:
+ * counts (device uint64[2], accumulated into, not cleared) += the node
+ * visits and the point-triangle tests of the build, each counted per voxel
+ * (a warp's visit counts once for every voxel it walks for).  The brute
+ * force counts N^3 * nf tests and no visits.  The grid is the same as
+ * mo_df_build_ex's; the counting build runs slower and is for measurement
+ * only.  No counterpart in the reference. */
+int mo_df_build_count(const float* V, int64_t nv, const int32_t* F, int64_t nf, int N,
+                      const double* params4, const MoDfOptions* opt, void* scratch, size_t scratch_bytes,
+                      float* grid_linear_out, int32_t* status_out, uint64_t* counts, void* stream);
 /* The smallest band that leaves DistanceFieldLoss unchanged for every input:
  * 0.2 + sqrt(3)/N + 1e-3.  UniformGrid::DistanceFloat (uniformgrid.cc:
  * 147-148) returns 0 when the in-range trilinear value exceeds 0.2; grid

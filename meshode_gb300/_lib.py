@@ -90,6 +90,7 @@ _SIGS = {
     "mo_df_method_for": (_I, [_I64, _I]),
     "mo_df_loss_band": (_F, [_I]),
     "mo_df_build_ex": (_I, [_P, _I64, _P, _I64, _I, _P, _P, _P, _SZ, _P, _P, _P]),
+    "mo_df_build_count": (_I, [_P, _I64, _P, _I64, _I, _P, _P, _P, _SZ, _P, _P, _P, _P]),
     "mo_df_build_noalloc": (_I, [_P, _I64, _P, _I64, _I, _P, _P, _P]),
     "mo_df_noalloc_scratch_capacity": (_SZ, []),
     "mo_df_tree_bytes": (_SZ, [_I64]),

@@ -307,10 +307,14 @@ __device__ __forceinline__ float2 obb_d2_2(float2 px, float2 py, float2 pz, floa
 // lanes of the warp call it together and walk the tree jointly (node and
 // triangle loads are warp-uniform broadcasts); lanes with valid == false
 // only follow.  stack: this warp's TRAV_STACK ints of shared memory.
-template <bool PAIR_TRIS = false>
+// COUNT: also add this warp's node visits and triangle tests, each times the
+// warp's valid voxels, to counts[0] and counts[1] (the measurement build,
+// mo_df_build_count; compiled out otherwise).
+template <bool PAIR_TRIS = false, bool COUNT = false>
 __device__ __forceinline__ float df_voxel_value(const float4* __restrict__ nodes, const float4* __restrict__ tris,
                                                 int ntri, int N, float band, float band2, int x, int y, int z,
-                                                bool valid, int* stack, int* __restrict__ status) {
+                                                bool valid, int* stack, int* __restrict__ status,
+                                                unsigned long long* __restrict__ counts = nullptr) {
     const int lane = threadIdx.x & 31;
     const float Nf = (float)N;
     const float px = __fdiv_rn((float)x, Nf), py = __fdiv_rn((float)y, Nf), pz = __fdiv_rn((float)z, Nf);
@@ -326,9 +330,11 @@ __device__ __forceinline__ float df_voxel_value(const float4* __restrict__ nodes
     // every distance below it.
     float lim = valid ? (init == FLT_MAX ? FLT_MAX : slack_bound(init)) : -1.0f;
     const unsigned FULL = 0xffffffffu;
+    unsigned long long n_visit = 0, n_test = 0;  // warp-uniform (COUNT only)
     if (ntri == 1) {
         const float t = tri_d2(px, py, pz, load_tri(tris, 0), best);
         if (valid && t < best) best = t;
+        if (COUNT) n_test = 1;
     } else {
         int sp = 0;
         int node = 0;
@@ -340,6 +346,7 @@ __device__ __forceinline__ float df_voxel_value(const float4* __restrict__ nodes
                 if (lane == 0) atomicOr(status, 4);
                 break;
             }
+            if (COUNT) ++n_visit;
             const float4* nd = nodes + NODE_F4 * (int64_t)node;
             const float4 l0 = __ldg(nd), l1 = __ldg(nd + 1), l2 = __ldg(nd + 2), l3 = __ldg(nd + 3);
             const float4 r0 = __ldg(nd + 4), r1 = __ldg(nd + 5), r2 = __ldg(nd + 6), r3 = __ldg(nd + 7);
@@ -351,6 +358,7 @@ __device__ __forceinline__ float df_voxel_value(const float4* __restrict__ nodes
             bool wr = __any_sync(FULL, dr < lim);
             // the opened buckets' triangles, left then right, one test body
             const int nl = wl ? cl : 0, nr = wr ? cr : 0;
+            if (COUNT) n_test += (unsigned long long)(nl + nr);
             // two triangles per test where both are non-degenerate
 #pragma unroll 1
             for (int k = 0; PAIR_TRIS && k < nl + nr; k += 2) {
@@ -405,15 +413,24 @@ __device__ __forceinline__ float df_voxel_value(const float4* __restrict__ nodes
             __syncwarp();
         }
     }
+    if (COUNT) {
+        const unsigned long long nvalid = (unsigned long long)__popc(__ballot_sync(FULL, valid));
+        if (lane == 0) {
+            atomicAdd(&counts[0], n_visit * nvalid);
+            atomicAdd(&counts[1], n_test * nvalid);
+        }
+    }
     return best < init ? __fsqrt_rn(best) : vb.value;
 }
 
 // The values of voxels (x, y, za) and (x, y, zb) of this lane, by one joint
 // walk of the warp (see df_voxel_value).
+template <bool COUNT = false>
 __device__ __forceinline__ float2 df_voxel_value2(const float4* __restrict__ nodes,
                                                   const float4* __restrict__ tris, int ntri, int N, float band,
                                                   float band2, int x, int y, int za, int zb, bool va, bool vb,
-                                                  int* stack, int* __restrict__ status) {
+                                                  int* stack, int* __restrict__ status,
+                                                  unsigned long long* __restrict__ counts = nullptr) {
     const int lane = threadIdx.x & 31;
     const float Nf = (float)N;
     const float fx = __fdiv_rn((float)x, Nf), fy = __fdiv_rn((float)y, Nf);
@@ -425,10 +442,12 @@ __device__ __forceinline__ float2 df_voxel_value2(const float4* __restrict__ nod
     float2 lim = make_float2(va ? (init.x == FLT_MAX ? FLT_MAX : slack_bound(init.x)) : -1.0f,
                              vb ? (init.y == FLT_MAX ? FLT_MAX : slack_bound(init.y)) : -1.0f);
     const unsigned FULL = 0xffffffffu;
+    unsigned long long n_visit = 0, n_test = 0;  // warp-uniform (COUNT only)
     if (ntri == 1) {
         const float2 t = tri_d2_2(px, py, pz, load_tri(tris, 0), best);
         if (va && t.x < best.x) best.x = t.x;
         if (vb && t.y < best.y) best.y = t.y;
+        if (COUNT) n_test = 1;
     } else {
         int sp = 0;
         int node = 0;
@@ -438,6 +457,7 @@ __device__ __forceinline__ float2 df_voxel_value2(const float4* __restrict__ nod
                 if (lane == 0) atomicOr(status, 4);
                 break;
             }
+            if (COUNT) ++n_visit;
             const float4* nd = nodes + NODE_F4 * (int64_t)node;
             const float4 l0 = __ldg(nd), l1 = __ldg(nd + 1), l2 = __ldg(nd + 2), l3 = __ldg(nd + 3);
             const float4 r0 = __ldg(nd + 4), r1 = __ldg(nd + 5), r2 = __ldg(nd + 6), r3 = __ldg(nd + 7);
@@ -448,6 +468,7 @@ __device__ __forceinline__ float2 df_voxel_value2(const float4* __restrict__ nod
             bool wl = __any_sync(FULL, dl.x < lim.x || dl.y < lim.y);
             bool wr = __any_sync(FULL, dr.x < lim.x || dr.y < lim.y);
             const int nl = wl ? cl : 0, nr = wr ? cr : 0;
+            if (COUNT) n_test += (unsigned long long)(nl + nr);
 #pragma unroll 1
             for (int k = 0; k < nl + nr; ++k) {
                 const int tri = k < nl ? ~L + k : ~R + (k - nl);
@@ -480,6 +501,14 @@ __device__ __forceinline__ float2 df_voxel_value2(const float4* __restrict__ nod
                 node = stack[--sp];
             }
             __syncwarp();
+        }
+    }
+    if (COUNT) {
+        const unsigned long long nvalid =
+            (unsigned long long)(__popc(__ballot_sync(FULL, va)) + __popc(__ballot_sync(FULL, vb)));
+        if (lane == 0) {
+            atomicAdd(&counts[0], n_visit * nvalid);
+            atomicAdd(&counts[1], n_test * nvalid);
         }
     }
     return make_float2(best.x < init.x ? __fsqrt_rn(best.x) : ba.value, best.y < init.y ? __fsqrt_rn(best.y) : bb.value);

@@ -558,11 +558,12 @@ __global__ void k_obb_nodes(const float4* __restrict__ nodes, const int2* __rest
 }
 
 // The full grid: one warp per packet of PX x PY x PZ voxels.
-template <int PX, int PY, int PZ, bool PAIR_TRIS>
+template <int PX, int PY, int PZ, bool PAIR_TRIS, bool COUNT = false>
 __global__ void __launch_bounds__(TRAV_WARPS * 32) k_df_lbvh(const float4* __restrict__ nodes,
                                                              const float4* __restrict__ tris, int ntri, int N,
                                                              float band, float band2, float* __restrict__ grid,
-                                                             int* __restrict__ status) {
+                                                             int* __restrict__ status,
+                                                             unsigned long long* __restrict__ counts) {
     __shared__ int stack[TRAV_WARPS][TRAV_STACK];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     static_assert(PX * PY * PZ == 32, "a packet is one warp");
@@ -572,16 +573,18 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) k_df_lbvh(const float4* __res
     const int ix = (int)(brick % bx), iy = (int)((brick / bx) % by), iz = (int)(brick / ((int64_t)bx * by));
     const int x = ix * PX + (lane % PX), y = iy * PY + ((lane / PX) % PY), z = iz * PZ + lane / (PX * PY);
     const bool valid = x < N && y < N && z < N;
-    const float v = df_voxel_value<PAIR_TRIS>(nodes, tris, ntri, N, band, band2, x, y, z, valid, stack[w], status);
+    const float v = df_voxel_value<PAIR_TRIS, COUNT>(nodes, tris, ntri, N, band, band2, x, y, z, valid, stack[w],
+                                                     status, counts);
     if (valid) grid[((int64_t)z * N + y) * N + x] = v;
 }
 
 // Two voxels per lane: the base packet PX x PY x PZ and the one PZ above it.
-template <int PX, int PY, int PZ>
+template <int PX, int PY, int PZ, bool COUNT = false>
 __global__ void __launch_bounds__(TRAV_WARPS * 32) k_df_lbvh2(const float4* __restrict__ nodes,
                                                               const float4* __restrict__ tris, int ntri, int N,
                                                               float band, float band2, float* __restrict__ grid,
-                                                              int* __restrict__ status) {
+                                                              int* __restrict__ status,
+                                                              unsigned long long* __restrict__ counts) {
     __shared__ int stack[TRAV_WARPS][TRAV_STACK];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     static_assert(PX * PY * PZ == 32, "a packet is one warp");
@@ -592,47 +595,56 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) k_df_lbvh2(const float4* __re
     const int x = ix * PX + (lane % PX), y = iy * PY + ((lane / PX) % PY);
     const int za = iz * 2 * PZ + lane / (PX * PY), zb = za + PZ;
     const bool va = x < N && y < N && za < N, vb = x < N && y < N && zb < N;
-    const float2 v = df_voxel_value2(nodes, tris, ntri, N, band, band2, x, y, za, zb, va, vb, stack[w], status);
+    const float2 v = df_voxel_value2<COUNT>(nodes, tris, ntri, N, band, band2, x, y, za, zb, va, vb, stack[w],
+                                            status, counts);
     if (va) grid[((int64_t)za * N + y) * N + x] = v.x;
     if (vb) grid[((int64_t)zb * N + y) * N + x] = v.y;
 }
 
 template <int PX, int PY, int PZ>
 static void launch_df_lbvh2_shape(const float4* nodes, const float4* tris, int ntri, int N, float band, float band2,
-                                  float* grid, int* status, cudaStream_t s) {
+                                  float* grid, int* status, unsigned long long* counts, cudaStream_t s) {
     const int64_t bricks = (int64_t)((N + PX - 1) / PX) * ((N + PY - 1) / PY) * ((N + 2 * PZ - 1) / (2 * PZ));
-    k_df_lbvh2<PX, PY, PZ><<<ceil_div(bricks, TRAV_WARPS), TRAV_WARPS * 32, 0, s>>>(nodes, tris, ntri, N, band,
-                                                                                  band2, grid, status);
+    if (counts)
+        k_df_lbvh2<PX, PY, PZ, true><<<ceil_div(bricks, TRAV_WARPS), TRAV_WARPS * 32, 0, s>>>(
+            nodes, tris, ntri, N, band, band2, grid, status, counts);
+    else
+        k_df_lbvh2<PX, PY, PZ><<<ceil_div(bricks, TRAV_WARPS), TRAV_WARPS * 32, 0, s>>>(
+            nodes, tris, ntri, N, band, band2, grid, status, nullptr);
     ::mo::note_launch();
 }
 
 template <int PX, int PY, int PZ, bool PAIR_TRIS = false>
 static void launch_df_lbvh_shape(const float4* nodes, const float4* tris, int ntri, int N, float band, float band2,
-                                 float* grid, int* status, cudaStream_t s) {
+                                 float* grid, int* status, unsigned long long* counts, cudaStream_t s) {
     const int64_t bricks = (int64_t)((N + PX - 1) / PX) * ((N + PY - 1) / PY) * ((N + PZ - 1) / PZ);
-    k_df_lbvh<PX, PY, PZ, PAIR_TRIS><<<ceil_div(bricks, TRAV_WARPS), TRAV_WARPS * 32, 0, s>>>(
-        nodes, tris, ntri, N, band, band2, grid, status);
+    if (counts)
+        k_df_lbvh<PX, PY, PZ, PAIR_TRIS, true><<<ceil_div(bricks, TRAV_WARPS), TRAV_WARPS * 32, 0, s>>>(
+            nodes, tris, ntri, N, band, band2, grid, status, counts);
+    else
+        k_df_lbvh<PX, PY, PZ, PAIR_TRIS><<<ceil_div(bricks, TRAV_WARPS), TRAV_WARPS * 32, 0, s>>>(
+            nodes, tris, ntri, N, band, band2, grid, status, nullptr);
     ::mo::note_launch();
 }
 
+// counts != NULL: the counting instantiation (node visits and triangle tests
+// per voxel into counts[0], counts[1]); it computes the same grid.
 static void launch_df_lbvh(int packet, const float4* nodes, const float4* tris, int ntri, int N, float band,
-                           float band2, float* grid, int* status, cudaStream_t s) {
+                           float band2, float* grid, int* status, unsigned long long* counts, cudaStream_t s) {
+#define MO_ARGS nodes, tris, ntri, N, band, band2, grid, status, counts, s
     switch (packet) {
-        case MO_PACKET_8x4x1: launch_df_lbvh_shape<8, 4, 1>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
-        case MO_PACKET_4x2x4: launch_df_lbvh_shape<4, 2, 4>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
-        case MO_PACKET_2x4x4: launch_df_lbvh_shape<2, 4, 4>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
-        case MO_PACKET_8x2x2: launch_df_lbvh_shape<8, 2, 2>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
-        case MO_PACKET_4x4x4: launch_df_lbvh2_shape<4, 4, 2>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
-        case MO_PACKET_2x4x8: launch_df_lbvh2_shape<2, 4, 4>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
-        case MO_PACKET_8x4x2: launch_df_lbvh2_shape<8, 4, 1>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
-        case MO_PACKET_4x4x2_TRI2:
-            launch_df_lbvh_shape<4, 4, 2, true>(nodes, tris, ntri, N, band, band2, grid, status, s);
-            break;
-        case MO_PACKET_2x4x4_TRI2:
-            launch_df_lbvh_shape<2, 4, 4, true>(nodes, tris, ntri, N, band, band2, grid, status, s);
-            break;
-        default: launch_df_lbvh_shape<4, 4, 2>(nodes, tris, ntri, N, band, band2, grid, status, s); break;
+        case MO_PACKET_8x4x1: launch_df_lbvh_shape<8, 4, 1>(MO_ARGS); break;
+        case MO_PACKET_4x2x4: launch_df_lbvh_shape<4, 2, 4>(MO_ARGS); break;
+        case MO_PACKET_2x4x4: launch_df_lbvh_shape<2, 4, 4>(MO_ARGS); break;
+        case MO_PACKET_8x2x2: launch_df_lbvh_shape<8, 2, 2>(MO_ARGS); break;
+        case MO_PACKET_4x4x4: launch_df_lbvh2_shape<4, 4, 2>(MO_ARGS); break;
+        case MO_PACKET_2x4x8: launch_df_lbvh2_shape<2, 4, 4>(MO_ARGS); break;
+        case MO_PACKET_8x4x2: launch_df_lbvh2_shape<8, 4, 1>(MO_ARGS); break;
+        case MO_PACKET_4x4x2_TRI2: launch_df_lbvh_shape<4, 4, 2, true>(MO_ARGS); break;
+        case MO_PACKET_2x4x4_TRI2: launch_df_lbvh_shape<2, 4, 4, true>(MO_ARGS); break;
+        default: launch_df_lbvh_shape<4, 4, 2>(MO_ARGS); break;
     }
+#undef MO_ARGS
 }
 
 // Brute force: each thread one voxel, triangles staged through shared memory.
@@ -839,9 +851,11 @@ extern "C" size_t mo_df_build_scratch_bytes(int64_t nv, int64_t nf, int N, int m
     return plan_scratch(nullptr, nv, nf, method).bytes;
 }
 
-extern "C" int mo_df_build_ex(const float* V, int64_t nv, const int32_t* F, int64_t nf, int N,
-                              const double* params4, const MoDfOptions* opt, void* scratch, size_t scratch_bytes,
-                              float* grid_out, int32_t* status_out, void* stream) {
+__global__ void k_add_u64(unsigned long long* __restrict__ c, unsigned long long v) { atomicAdd(c, v); }
+
+static int df_build_impl(const float* V, int64_t nv, const int32_t* F, int64_t nf, int N, const double* params4,
+                         const MoDfOptions* opt, void* scratch, size_t scratch_bytes, float* grid_out,
+                         int32_t* status_out, unsigned long long* counts, void* stream) {
     int method = opt ? opt->method : MO_DF_AUTO;
     const int packet = opt ? opt->packet : MO_PACKET_4x4x2;
     const float band = opt ? opt->band : 0.0f;
@@ -884,10 +898,14 @@ extern "C" int mo_df_build_ex(const float* V, int64_t nv, const int32_t* F, int6
             const int64_t nvox = (int64_t)N * N * N;
             k_df_brute<<<ceil_div(nvox, BF_THREADS), BF_THREADS, 0, s>>>(S.tris, (int)nf, N, band, band2, grid_out);
             ::mo::note_launch();
+            if (counts) {  // every voxel tests every triangle
+                k_add_u64<<<1, 1, 0, s>>>(counts + 1, (unsigned long long)nvox * (unsigned long long)nf);
+                ::mo::note_launch();
+            }
         } else {
             e = issue_tree(S, F, nv, nf, st, s);
             if (e != cudaSuccess) { fail(e, "LBVH build"); break; }
-            launch_df_lbvh(packet, S.tnodes, S.tris, (int)nf, N, band, band2, grid_out, st, s);
+            launch_df_lbvh(packet, S.tnodes, S.tris, (int)nf, N, band, band2, grid_out, st, counts, s);
         }
         e = cudaGetLastError();
         if (e != cudaSuccess) { fail(e, "df build kernels"); break; }
@@ -903,6 +921,21 @@ extern "C" int mo_df_build_ex(const float* V, int64_t nv, const int32_t* F, int6
     }
     if (owned) cudaFreeAsync(owned, s);
     return rc;
+}
+
+extern "C" int mo_df_build_ex(const float* V, int64_t nv, const int32_t* F, int64_t nf, int N,
+                              const double* params4, const MoDfOptions* opt, void* scratch, size_t scratch_bytes,
+                              float* grid_out, int32_t* status_out, void* stream) {
+    return df_build_impl(V, nv, F, nf, N, params4, opt, scratch, scratch_bytes, grid_out, status_out, nullptr,
+                         stream);
+}
+
+extern "C" int mo_df_build_count(const float* V, int64_t nv, const int32_t* F, int64_t nf, int N,
+                                 const double* params4, const MoDfOptions* opt, void* scratch, size_t scratch_bytes,
+                                 float* grid_out, int32_t* status_out, uint64_t* counts, void* stream) {
+    MO_CHECK_ARG(counts, "null counts pointer");
+    return df_build_impl(V, nv, F, nf, N, params4, opt, scratch, scratch_bytes, grid_out, status_out,
+                         reinterpret_cast<unsigned long long*>(counts), stream);
 }
 
 extern "C" int mo_df_build(const float* V, int64_t nv, const int32_t* F, int64_t nf, int N, const double* params4,

@@ -84,3 +84,41 @@ def test_serving_with_tuner_is_identical(cuda, tmp_path):
         assert torch.equal(x.out, y.out)
     reloaded = autotune.Autotuner(cache_path=str(tmp_path / "tune.json"))
     assert reloaded.table == tuner.table
+
+
+def test_counting_build_same_grid_and_counts(cuda):
+    """mo_df_build_count (the measurement build of the bench's DF roofline)
+    gives every packet shape's grid bit for bit, with and without the band;
+    the brute force counts N^3 * triangles tests and no visits; the LBVH
+    walks count visits and far fewer tests; counts accumulate."""
+    rng = np.random.Generator(np.random.PCG64(3))
+    V, F = meshgen.icosphere(4)
+    T = torch.from_numpy(meshgen.displace(V, rng).astype(np.float32)).to(cuda)
+    Fd = torch.from_numpy(F.astype(np.int32)).to(cuda)
+    s = L.stream_ptr()
+    bbox = torch.empty(6, dtype=torch.int32, device=cuda)
+    prm = torch.empty(4, dtype=torch.float64, device=cuda)
+    L.call("mo_bbox", L.ptr(T), T.shape[0], L.ptr(bbox), s)
+    L.call("mo_norm_params", L.ptr(bbox), L.ptr(prm), s)
+    N = 29
+    nf = Fd.shape[0]
+    for band in (0.0, L.lib().mo_df_loss_band(N)):
+        cands = [(L.MO_DF_LBVH, p) for p in autotune.PACKETS.values()] + [(L.MO_DF_BRUTE, 0)]
+        for method, packet in cands:
+            opt = L.MoDfOptions(method, packet, band)
+            g0 = torch.empty(N ** 3, dtype=torch.float32, device=cuda)
+            g1 = torch.full((N ** 3,), float("nan"), dtype=torch.float32, device=cuda)
+            c = torch.zeros(2, dtype=torch.int64, device=cuda)
+            L.call("mo_df_build_ex", L.ptr(T), T.shape[0], L.ptr(Fd), nf, N, L.ptr(prm), ctypes.byref(opt),
+                   None, 0, L.ptr(g0), None, s)
+            L.call("mo_df_build_count", L.ptr(T), T.shape[0], L.ptr(Fd), nf, N, L.ptr(prm), ctypes.byref(opt),
+                   None, 0, L.ptr(g1), None, L.ptr(c), s)
+            assert torch.equal(g0, g1), (method, packet, band)
+            visits, tests = c.cpu().tolist()
+            if method == L.MO_DF_BRUTE:
+                assert (visits, tests) == (0, N ** 3 * nf)
+            else:
+                assert visits > 0 and 0 < tests < N ** 3 * nf // 20, (packet, visits, tests)
+                L.call("mo_df_build_count", L.ptr(T), T.shape[0], L.ptr(Fd), nf, N, L.ptr(prm),
+                       ctypes.byref(opt), None, 0, L.ptr(g1), None, L.ptr(c), s)
+                assert c.cpu().tolist() == [2 * visits, 2 * tests]

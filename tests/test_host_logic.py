@@ -112,3 +112,24 @@ def test_autotune_buckets():
     from meshode_gb300 import autotune
     assert autotune.t_bucket(5000) == 12 and autotune.t_bucket(8192) == 13
     assert autotune.v_bucket(1) == 0 and autotune.v_bucket(100000) == 16
+
+
+def test_cpu_baseline_strata():
+    """bench.py's CPU sample: one request from each of the 12 strata (grid x
+    source-vertex tercile x target-triangle half) of the 512-request stream,
+    and the stream-weighted estimate (exact for a constant cost; a stratum's
+    weight is its share of the stream)."""
+    import argparse
+    import bench
+    specs, _ = bench.make_stream(argparse.Namespace(requests=512, req_steps=500), 5)
+    strata = bench.cpu_strata(specs)
+    assert len(strata) == 12 and sum(len(v) for v in strata.values()) == 512
+    ids = bench.cpu_sample_ids(specs)
+    assert len(ids) == 12 and len(set(ids)) == 12
+    assert sorted(strata) == [k for k in sorted(strata) if any(i in strata[k] for i in ids)]
+    assert abs(bench.stream_mean_seconds(specs, {i: [2.0] for i in ids}) - 2.0) < 1e-12
+    # cost proportional to the stratum's index: the estimate is the share-weighted mean
+    keys = sorted(strata)
+    cost = {i: [float(keys.index(k))] for k in keys for i in ids if i in strata[k]}
+    want = sum(len(strata[k]) / 512 * keys.index(k) for k in keys)
+    assert abs(bench.stream_mean_seconds(specs, cost) - want) < 1e-12
