@@ -754,9 +754,14 @@ def ode_config():
             "stored_activations_ms_per_iteration": stored, "stored_activations_peak_extra_mem_gb": stored_mem / 1e9,
             "torch_autograd_ms_per_iteration": plain, "torch_autograd_peak_extra_mem_gb": plain_mem / 1e9,
             "tflops": flops / (ours * 1e-3) / 1e12,
+            "fp32_peak_tflops": 152 * 128 * 2 * 2.07e9 / 1e12,
+            "kernels": "mo_mlp_fwd (fused 4-layer evaluation + RK4 update per 64-vertex tile), mo_mlp_bwd "
+                       "(fused vector-Jacobian product), mo_mlp_wgrad (split-K 256x256 weight gradients): "
+                       "FP32 SIMT with packed FFMA2, no library GEMM",
             "note": "checkpointed adjoint: recomputes each RK4 step's activations (4/3 of the FLOPs) to hold "
                     "one step's activations instead of all 80 stage evaluations'; stored_activations: the same "
-                    "fit keeping them (same gradients bit for bit)"}
+                    "fit keeping them (same gradients bit for bit); torch_autograd: the same fp32 model through "
+                    "torch (cuBLAS) autograd, every activation stored"}
 
 
 # ---------------------------------------------------------------------------

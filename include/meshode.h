@@ -549,29 +549,45 @@ int mo_solve_linear(float* V, int64_t nv, const int32_t* F, int64_t nf, const in
 
 /* ------------------------------------------------------------------------
  * Velocity-field ODE deformation (the NeuralODE variant,
- * src/python/layers/neuralode_fast.py:7-64; here 3 -> m -> m -> m -> 3 with
- * softplus and fixed-step RK4).  The m x m layers are plain GEMMs done by
- * the caller (cuBLAS); these are the kernels around them.
+ * src/python/layers/neuralode_fast.py:10-31,55-57; here an autonomous
+ * 3 -> 256 -> 256 -> 256 -> 3 softplus MLP integrated by fixed-step RK4).
+ * Fused FP32 kernels over 64-vertex tiles; a narrower MLP runs zero-padded
+ * to mo_mlp_width().  Weights: W1 [M,3], b1 [M], W2 and W3 [M,M] (row =
+ * output unit), b2, b3 [M], W4 [3,M], b4 [3], all row-major.
  * ------------------------------------------------------------------------ */
-/* z = x W1^T + b1, h = softplus(z): x [n,3], W1 [m,3], z and h [n,m]
- * (z may be NULL when only h is needed). */
-int mo_mlp_in(const float* x, int64_t n, const float* W1, const float* b1, int m, float* z, float* h,
-              void* stream);
-/* In place z += b (per column), h = softplus(z): z, h [n,m], b [m]. */
-int mo_bias_softplus(float* z, int64_t n, int m, const float* b, float* h, void* stream);
-/* k = h W4^T + b4 (h [n,m], W4 [3,m]); u = x + a*k; acc = (init_acc ? x : acc)
- * + w*k -- one RK4 stage's output and update; k, u or acc may be NULL. */
-int mo_mlp_out_rk4(const float* h, int64_t n, int m, const float* W4, const float* b4, const float* x,
-                   float a, float w, int init_acc, float* k, float* u, float* acc, void* stream);
-/* g_z = (g_out W4) * sigmoid(z): the output layer's backward through the last
- * softplus (g_out [n,3], W4 [3,m], z and g_z [n,m]). */
-int mo_mlp_out_bwd(const float* g_out, int64_t n, int m, const float* W4, const float* z, float* g_z,
-                   void* stream);
-/* In place g *= sigmoid(z) (softplus' = sigmoid). */
-int mo_softplus_bwd(float* g, const float* z, int64_t count, void* stream);
-/* g_x = g_z W1 (accumulate != 0: g_x += g_z W1); g_z [n,m], W1 [m,3]. */
-int mo_mlp_in_bwd(const float* g_z, int64_t n, int m, const float* W1, float* g_x, int accumulate,
-                  void* stream);
+/* The kernels' hidden width M (256). */
+int mo_mlp_width(void);
+/* 64-vertex tiles of n rows (the grid of mo_mlp_fwd / mo_mlp_bwd). */
+int64_t mo_mlp_tiles(int64_t n);
+/* Floats in one partial row of mo_mlp_bwd (one row per warp, 8 per tile). */
+int mo_mlp_partial_floats(void);
+/* WT = W^T for an M x M matrix (the forward takes W2^T and W3^T). */
+int mo_mlp_transpose(const float* W, float* WT, void* stream);
+/* One MLP evaluation k = f(u) of n rows with its RK4 stage update:
+ * unext = x + a*k (unext may be NULL), acc = (init_acc ? x : acc) + w*k.
+ * store (may be NULL): Z1, H1, Z2, H2, Z3, H3 (pre- and post-softplus of the
+ * three hidden layers, each [n,M]) at store + i*astride, for mo_mlp_bwd. */
+int mo_mlp_fwd(const float* u, const float* x, int64_t n, const float* W1, const float* b1, const float* W2T,
+               const float* b2, const float* W3T, const float* b3, const float* W4, const float* b4, float a,
+               float w, int init_acc, float* unext, float* acc, float* store, int64_t astride, void* stream);
+/* The vector-Jacobian product of one evaluation for dL/dk = gk [n,3], from
+ * its stored activations: gu [n,3] = dL/du; gz3, gz2 [n,M] = dL/dZ3, dL/dZ2
+ * (for mo_mlp_wgrad); partial gets one row of mo_mlp_partial_floats() per
+ * warp (8 * mo_mlp_tiles(n) rows) holding that warp's dW4, db4, db3, db2,
+ * db1, dW1 terms, for mo_mlp_partial_reduce. */
+int mo_mlp_bwd(const float* gk, const float* u, int64_t n, const float* W1, const float* W2, const float* W3,
+               const float* W4, const float* store, int64_t astride, float* gz3, float* gz2, float* gu,
+               float* partial, void* stream);
+/* dW4 [3,M], db4 [3], db3, db2, db1 [M], dW1 [M,3] += the sums of `rows`
+ * partial rows, in row order. */
+int mo_mlp_partial_reduce(const float* partial, int64_t rows, float* dW4, float* db4, float* db3, float* db2,
+                          float* db1, float* dW1, void* stream);
+/* dW [M,M] += A^T B (A, B [rows,M]: dW[o][i] = sum_r A[r][o] B[r][i]),
+ * split over rows into `splits` partial sums (partial:
+ * mo_mlp_wgrad_partial_bytes(splits)) added in split order. */
+size_t mo_mlp_wgrad_partial_bytes(int splits);
+int mo_mlp_wgrad(const float* A, const float* B, int64_t rows, int splits, float* partial, float* dW,
+                 void* stream);
 
 /* sizeof(MoPair) and sizeof(MoTile) as compiled (host pointers), so that
  * bindings in other languages can check their struct layout. */

@@ -122,12 +122,15 @@ _SIGS = {
     "mo_fused_step_on_demand": (_I, [_P, _P, _P, _I, _I, _P, _I, _P]),
     "mo_pair_loss": (_I, [_P, _I, _I, _I, _P, _P, _P]),
     "mo_abi_sizes": (_I, [ctypes.POINTER(_SZ), ctypes.POINTER(_SZ)]),
-    "mo_mlp_in": (_I, [_P, _I64, _P, _P, _I, _P, _P, _P]),
-    "mo_bias_softplus": (_I, [_P, _I64, _I, _P, _P, _P]),
-    "mo_mlp_out_rk4": (_I, [_P, _I64, _I, _P, _P, _P, _F, _F, _I, _P, _P, _P, _P]),
-    "mo_mlp_out_bwd": (_I, [_P, _I64, _I, _P, _P, _P, _P]),
-    "mo_softplus_bwd": (_I, [_P, _P, _I64, _P]),
-    "mo_mlp_in_bwd": (_I, [_P, _I64, _I, _P, _P, _I, _P]),
+    "mo_mlp_width": (_I, []),
+    "mo_mlp_tiles": (_I64, [_I64]),
+    "mo_mlp_partial_floats": (_I, []),
+    "mo_mlp_transpose": (_I, [_P, _P, _P]),
+    "mo_mlp_fwd": (_I, [_P, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _F, _F, _I, _P, _P, _P, _I64, _P]),
+    "mo_mlp_bwd": (_I, [_P, _P, _I64, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _P]),
+    "mo_mlp_partial_reduce": (_I, [_P, _I64, _P, _P, _P, _P, _P, _P, _P]),
+    "mo_mlp_wgrad_partial_bytes": (_SZ, [_I]),
+    "mo_mlp_wgrad": (_I, [_P, _P, _I64, _I, _P, _P, _P]),
     "mo_pack_pos": (_I, [_P, _I64, _P, _P]),
     "mo_unpack_pos": (_I, [_P, _I64, _P, _P]),
     "mo_nn_scratch_bytes": (_SZ, [_I64, _I64]),

@@ -18,10 +18,11 @@ the graph/DF losses, back-propagating through the stored RK4 graph.  Here:
   from the forward instead: plain autograd's memory, no recompute, the same
   gradients bit for bit).
 
-The m x m layers are cuBLAS fp32 GEMMs (TF32 must be off:
-``torch.backends.cuda.matmul.allow_tf32 = False``, torch's default); the
-3-wide layers, bias + softplus epilogues, RK4 stage updates and the backward
-gates are libmeshode kernels (mo_mlp_*, mo_bias_softplus, mo_softplus_bwd).
+Every evaluation of the MLP is one fused libmeshode kernel (mo_mlp_fwd:
+the four layers of a 64-vertex tile with its activations kept on chip, and
+the RK4 stage update), its vector-Jacobian product another (mo_mlp_bwd), and
+the 256x256 weight gradients a split-K kernel over the four stages of a step
+(mo_mlp_wgrad); all FP32 (packed FFMA2), no library GEMM.
 """
 import math
 
@@ -47,121 +48,196 @@ def init_params(hidden=256, seed=4, device="cuda"):
     return out
 
 
-class _Stage:
-    __slots__ = ("u", "z1", "h1", "z2", "h2", "z3", "h3")
+MLP_WIDTH = 256  # the fused kernels' hidden width; narrower MLPs run zero-padded
 
 
-def _stage(params, u, x, a, w, init_acc, unext, acc, store):
-    """One MLP evaluation k = f(u) fused with the RK4 update
-    unext = x + a*k, acc = (init ? x : acc) + w*k."""
-    W1, b1, W2, b2, W3, b3, W4, b4 = params
-    n, m = u.shape[0], W1.shape[0]
-    s = stream_ptr()
-    z1 = torch.empty(n, m, dtype=torch.float32, device=u.device) if store else None
-    h1 = torch.empty(n, m, dtype=torch.float32, device=u.device)
-    call("mo_mlp_in", ptr(u), n, ptr(W1), ptr(b1), m, ptr(z1), ptr(h1), s)
-    z2 = torch.matmul(h1, W2.t())
-    h2 = torch.empty_like(z2)
-    call("mo_bias_softplus", ptr(z2), n, m, ptr(b2), ptr(h2), s)
-    z3 = torch.matmul(h2, W3.t())
-    h3 = torch.empty_like(z3)
-    call("mo_bias_softplus", ptr(z3), n, m, ptr(b3), ptr(h3), s)
-    call("mo_mlp_out_rk4", ptr(h3), n, m, ptr(W4), ptr(b4), ptr(x), float(a), float(w), int(init_acc), None,
-         ptr(unext), ptr(acc), s)
-    if not store:
-        return None
-    st = _Stage()
-    st.u, st.z1, st.h1, st.z2, st.h2, st.z3, st.h3 = u, z1, h1, z2, h2, z3, h3
-    return st
+class _Packed:
+    """The parameters as the fused kernels take them: zero-padded to the
+    kernels' width (exact: a padded unit's pre-activation and outgoing
+    weights are 0), with W2 and W3 also transposed for the forward."""
+
+    def __init__(self, params):
+        W1, b1, W2, b2, W3, b3, W4, b4 = [p.detach() for p in params]
+        m = W1.shape[0]
+        M = L.lib().mo_mlp_width()
+        if m > M:
+            raise RuntimeError("hidden width %d exceeds the fused kernels' %d" % (m, M))
+        self.m, self.M = m, M
+        dev = W1.device
+
+        def pad(t, shape):
+            out = torch.zeros(shape, dtype=torch.float32, device=dev)
+            out[tuple(slice(0, k) for k in t.shape)] = t
+            return out
+
+        self.W1, self.b1 = pad(W1, (M, 3)), pad(b1, (M,))
+        self.W2, self.b2 = pad(W2, (M, M)), pad(b2, (M,))
+        self.W3, self.b3 = pad(W3, (M, M)), pad(b3, (M,))
+        self.W4, self.b4 = pad(W4, (3, M)), b4.contiguous().float()
+        self.W2T = torch.empty_like(self.W2)
+        self.W3T = torch.empty_like(self.W3)
+        s = stream_ptr()
+        call("mo_mlp_transpose", ptr(self.W2), ptr(self.W2T), s)
+        call("mo_mlp_transpose", ptr(self.W3), ptr(self.W3T), s)
+
+    def grads(self):
+        M = self.M
+        return [torch.zeros(sh, dtype=torch.float32, device=self.W1.device)
+                for sh in ((M, 3), (M,), (M, M), (M,), (M, M), (M,), (3, M), (3,))]
+
+    def unpad(self, g):
+        m = self.m
+        return [g[0][:m].contiguous(), g[1][:m].contiguous(), g[2][:m, :m].contiguous(), g[3][:m].contiguous(),
+                g[4][:m, :m].contiguous(), g[5][:m].contiguous(), g[6][:, :m].contiguous(), g[7]]
 
 
-def _rk4_step(params, x, h, store=False):
-    """One classic RK4 step; returns (x_next, [4 stage records] or None)."""
+def _fwd(P, u, x, a, w, init_acc, unext, acc, store=None, astride=0):
+    """One fused MLP evaluation k = f(u) with the RK4 update
+    unext = x + a*k, acc = (init ? x : acc) + w*k (mo_mlp_fwd); store: the
+    stage's Z1 H1 Z2 H2 Z3 H3 at stride astride."""
+    call("mo_mlp_fwd", ptr(u), ptr(x), u.shape[0], ptr(P.W1), ptr(P.b1), ptr(P.W2T), ptr(P.b2), ptr(P.W3T),
+         ptr(P.b3), ptr(P.W4), ptr(P.b4), float(a), float(w), int(init_acc), ptr(unext), ptr(acc), ptr(store),
+         int(astride), stream_ptr())
+
+
+class _StepStore:
+    """The activations of one RK4 step's four evaluations:
+    act [6][4][n][M] (Z1 H1 Z2 H2 Z3 H3 of stages 1..4) and the stage
+    inputs u2..u4."""
+
+    def __init__(self, n, M, dev):
+        self.n, self.M = n, M
+        self.act = torch.empty(6 * 4 * n * M, dtype=torch.float32, device=dev)
+        self.u = [None, torch.empty(n, 3, dtype=torch.float32, device=dev),
+                  torch.empty(n, 3, dtype=torch.float32, device=dev), torch.empty(n, 3, dtype=torch.float32, device=dev)]
+
+    def stage(self, s):
+        return self.act[s * self.n * self.M:], 4 * self.n * self.M
+
+    def array(self, a):
+        """Array a (0 Z1, 1 H1, 2 Z2, 3 H2, 4 Z3, 5 H3) of all four stages, [4n, M]."""
+        return self.act[a * 4 * self.n * self.M:(a + 1) * 4 * self.n * self.M]
+
+
+def _rk4_step(P, x, h, st=None):
+    """One classic RK4 step of the fused evaluations; with st, the stages'
+    activations and inputs are kept there.  Returns x_next."""
     acc = torch.empty_like(x)
-    u2, u3, u4 = torch.empty_like(x), torch.empty_like(x), torch.empty_like(x)
-    s1 = _stage(params, x, x, h / 2, h / 6, 1, u2, acc, store)
-    s2 = _stage(params, u2, x, h / 2, h / 3, 0, u3, acc, store)
-    s3 = _stage(params, u3, x, h, h / 3, 0, u4, acc, store)
-    s4 = _stage(params, u4, x, 0.0, h / 6, 0, None, acc, store)
-    return acc, ([s1, s2, s3, s4] if store else None)
+    if st is None:
+        u2, u3, u4 = torch.empty_like(x), torch.empty_like(x), torch.empty_like(x)
+    else:
+        u2, u3, u4 = st.u[1], st.u[2], st.u[3]
+    ss = [st.stage(k) if st is not None else (None, 0) for k in range(4)]
+    _fwd(P, x, x, h / 2, h / 6, 1, u2, acc, *ss[0])
+    _fwd(P, u2, x, h / 2, h / 3, 0, u3, acc, *ss[1])
+    _fwd(P, u3, x, h, h / 3, 0, u4, acc, *ss[2])
+    _fwd(P, u4, x, 0.0, h / 6, 0, None, acc, *ss[3])
+    return acc
 
 
-def _vjp(params, grads, st, g_out):
-    """Back-propagate g_out = dL/dk through one MLP evaluation; accumulates
-    the parameter gradients into `grads`, returns dL/du."""
-    W1, b1, W2, b2, W3, b3, W4, b4 = params
-    dW1, db1, dW2, db2, dW3, db3, dW4, db4 = grads
-    n, m = st.u.shape[0], W1.shape[0]
-    s = stream_ptr()
-    dW4.addmm_(g_out.t(), st.h3)
-    db4.add_(g_out.sum(0))
-    g_z3 = torch.empty(n, m, dtype=torch.float32, device=g_out.device)
-    call("mo_mlp_out_bwd", ptr(g_out), n, m, ptr(W4), ptr(st.z3), ptr(g_z3), s)
-    dW3.addmm_(g_z3.t(), st.h2)
-    db3.add_(g_z3.sum(0))
-    g_z2 = torch.matmul(g_z3, W3)
-    call("mo_softplus_bwd", ptr(g_z2), ptr(st.z2), n * m, s)
-    dW2.addmm_(g_z2.t(), st.h1)
-    db2.add_(g_z2.sum(0))
-    g_z1 = torch.matmul(g_z2, W2)
-    call("mo_softplus_bwd", ptr(g_z1), ptr(st.z1), n * m, s)
-    dW1.addmm_(g_z1.t(), st.u)
-    db1.add_(g_z1.sum(0))
-    g_u = torch.empty(n, 3, dtype=torch.float32, device=g_out.device)
-    call("mo_mlp_in_bwd", ptr(g_z1), n, m, ptr(W1), ptr(g_u), 0, s)
-    return g_u
+class _Backward:
+    """Work buffers of the adjoint: the stage gradients g_z3, g_z2 of the
+    four evaluations of a step ([2][4][n][M]), the per-warp partial rows of
+    the small gradients and the split partials of the weight gradients."""
+
+    def __init__(self, n, M, dev):
+        lib = L.lib()
+        self.n, self.M = n, M
+        self.tiles = int(lib.mo_mlp_tiles(n))
+        self.pw = int(lib.mo_mlp_partial_floats())
+        self.gz = torch.empty(2 * 4 * n * M, dtype=torch.float32, device=dev)
+        self.partial = torch.empty(4 * self.tiles * 8 * self.pw, dtype=torch.float32, device=dev)
+        self.splits = max(1, min(2 * torch.cuda.get_device_properties(dev).multi_processor_count // 4,
+                                 (4 * n) // 256))
+        self.wpart = torch.empty(int(lib.mo_mlp_wgrad_partial_bytes(self.splits)) // 4, dtype=torch.float32,
+                                 device=dev)
+        self.gu = [torch.empty(n, 3, dtype=torch.float32, device=dev) for _ in range(4)]
+
+    def stage_vjp(self, P, st, s, u, gk):
+        """dL/du of evaluation s (0..3) of the step for dL/dk = gk."""
+        n, M = self.n, self.M
+        act, astride = st.stage(s)
+        gz3 = self.gz[s * n * M:]
+        gz2 = self.gz[(4 + s) * n * M:]
+        part = self.partial[s * self.tiles * 8 * self.pw:]
+        call("mo_mlp_bwd", ptr(gk), ptr(u), n, ptr(P.W1), ptr(P.W2), ptr(P.W3), ptr(P.W4), ptr(act), int(astride),
+             ptr(gz3), ptr(gz2), ptr(self.gu[s]), ptr(part), stream_ptr())
+        return self.gu[s]
+
+    def weights(self, st, grads):
+        """The parameter gradients of the step's four evaluations, added to grads."""
+        n, M = self.n, self.M
+        dW1, db1, dW2, db2, dW3, db3, dW4, db4 = grads
+        s = stream_ptr()
+        call("mo_mlp_partial_reduce", ptr(self.partial), 4 * self.tiles * 8, ptr(dW4), ptr(db4), ptr(db3),
+             ptr(db2), ptr(db1), ptr(dW1), s)
+        call("mo_mlp_wgrad", ptr(self.gz), ptr(st.array(3)), 4 * n, self.splits, ptr(self.wpart), ptr(dW3), s)
+        call("mo_mlp_wgrad", ptr(self.gz[4 * n * M:]), ptr(st.array(1)), 4 * n, self.splits, ptr(self.wpart),
+             ptr(dW2), s)
 
 
 class ODEFlow(Function):
     """x(1) = RK4^steps(x(0)) under the velocity MLP, with an adjoint
-    backward.  store=False: checkpointed (states at step starts kept, each
-    step's stage activations recomputed in the backward: one step's
-    activations in memory); store=True: every stage's activations kept from
-    the forward (the memory of plain autograd, no recompute).  Both give the
-    same gradients bit for bit (the recompute repeats the same kernels)."""
+    backward on the fused kernels.  store=False: checkpointed (states at
+    step starts kept, each step's stage activations recomputed in the
+    backward: one step's activations in memory); store=True: every step's
+    activations kept from the forward (no recompute).  Both give the same
+    gradients bit for bit (the recompute repeats the same kernels)."""
 
     @staticmethod
     def forward(ctx, x0, steps, store, W1, b1, W2, b2, W3, b3, W4, b4):
-        params = [t.detach().contiguous() for t in (W1, b1, W2, b2, W3, b3, W4, b4)]
+        P = _Packed((W1, b1, W2, b2, W3, b3, W4, b4))
         steps = int(steps)
         h = 1.0 / steps
-        x = x0.detach().contiguous()
-        ckpt = torch.empty(steps, x.shape[0], 3, dtype=torch.float32, device=x.device)
-        ctx.stages = [] if store else None
+        x = x0.detach().contiguous().float()
+        n = x.shape[0]
+        ckpt = torch.empty(steps, n, 3, dtype=torch.float32, device=x.device)
+        ctx.stores = [] if store else None
         for k in range(steps):
             ckpt[k].copy_(x)
-            x, st = _rk4_step(params, x, h, store=bool(store))
+            st = _StepStore(n, P.M, x.device) if store else None
+            x = _rk4_step(P, x, h, st)
             if store:
-                ctx.stages.append(st)
-        ctx.save_for_backward(ckpt, *params)
+                ctx.stores.append(st)
+        ctx.P = P
+        ctx.save_for_backward(ckpt)
         ctx.steps = steps
         return x
 
     @staticmethod
     def backward(ctx, a_out):
-        ckpt, *params = ctx.saved_tensors
+        (ckpt,) = ctx.saved_tensors
+        P = ctx.P
         steps = ctx.steps
         h = 1.0 / steps
-        grads = [torch.zeros_like(p) for p in params]
+        n = ckpt.shape[1]
+        grads = P.grads()
         a = a_out.contiguous().float()
+        B = _Backward(n, P.M, a.device)
+        work = None if ctx.stores is not None else _StepStore(n, P.M, a.device)
         for k in reversed(range(steps)):
-            if ctx.stages is not None:
-                st = ctx.stages[k]
-                ctx.stages[k] = None  # freed as the backward passes it
+            xk = ckpt[k]
+            if ctx.stores is not None:
+                st = ctx.stores[k]
+                ctx.stores[k] = None  # freed as the backward passes it
             else:
-                _, st = _rk4_step(params, ckpt[k], h, store=True)
+                st = work
+                _rk4_step(P, xk, h, st)
+            us = [xk, st.u[1], st.u[2], st.u[3]]
             dk4 = a * (h / 6)
-            g4 = _vjp(params, grads, st[3], dk4)
+            g4 = B.stage_vjp(P, st, 3, us[3], dk4)
             dx = a + g4
-            g3 = _vjp(params, grads, st[2], a * (h / 3) + h * g4)
+            g3 = B.stage_vjp(P, st, 2, us[2], a * (h / 3) + h * g4)
             dx += g3
-            g2 = _vjp(params, grads, st[1], a * (h / 3) + (h / 2) * g3)
+            g2 = B.stage_vjp(P, st, 1, us[1], a * (h / 3) + (h / 2) * g3)
             dx += g2
-            g1 = _vjp(params, grads, st[0], a * (h / 6) + (h / 2) * g2)
+            g1 = B.stage_vjp(P, st, 0, us[0], a * (h / 6) + (h / 2) * g2)
             dx += g1
+            B.weights(st, grads)
             a = dx
-        ctx.stages = None
-        return (a, None, None) + tuple(grads)
+        ctx.stores = None
+        ctx.P = None
+        return (a, None, None) + tuple(P.unpad(grads))
 
 
 class FitLossFunction(Function):
@@ -191,9 +267,6 @@ class NeuralODEDeformer:
     def __init__(self, src_V, src_F, tar_V, tar_F, grid_resolution=128, rigidity=0.1, hidden=256, steps=20,
                  seed=4, lr=1e-3, store_activations=False):
         L.require_cuda()
-        if torch.backends.cuda.matmul.allow_tf32:
-            raise RuntimeError("TF32 matmul is enabled; the ODE fit needs fp32 GEMMs "
-                               "(torch.backends.cuda.matmul.allow_tf32 = False)")
         dev = torch.device("cuda", torch.cuda.current_device())
         self.pid = PD.InitializeDeformTemplate(tar_V, tar_F, 0, grid_resolution)
         self.x0 = src_V.detach().to(dev).float().contiguous().clone()

@@ -1,4 +1,6 @@
-"""Continuous-batching serving loop on the GPU.
+"""Continuous-batching serving loop on the GPU, through the native pool
+(mo_pool_*, the product) and the Python engine that restates its schedule
+over the same kernels (kept as the tests' reference schedule).
 
 * Every request's result is bit-identical alone and inside the mixed stream
   (each pair's arithmetic depends only on its own state).
@@ -10,7 +12,7 @@ import numpy as np
 import pytest
 import torch
 
-from meshode_gb300 import fused, meshgen, serving
+from meshode_gb300 import fused, meshgen, pool, serving
 from meshode_gb300 import pyDeform as PD
 
 pytestmark = pytest.mark.gpu
@@ -28,10 +30,15 @@ def _fresh(reqs):
             for r in reqs]
 
 
-def test_alone_vs_mix_and_realtime(cuda):
+def _engine(kind, **kw):
+    return pool.NativePool(**kw) if kind == "native" else serving.ServingEngine(**kw)
+
+
+@pytest.mark.parametrize("kind", ["native", "python"])
+def test_alone_vs_mix_and_realtime(cuda, kind):
     specs, meshes = _stream()
     base = serving.requests_from_meshes(meshes, specs, device=None, pin=True)
-    eng = serving.ServingEngine(group_steps=8, max_building=3)
+    eng = _engine(kind, group_steps=8, max_building=3)
     mix = _fresh(base)
     eng.run(mix)
     assert all(r.error is None for r in mix)
@@ -42,16 +49,17 @@ def test_alone_vs_mix_and_realtime(cuda):
         assert b.latency is not None and b.latency > 0
     for r in (mix[0], mix[3], mix[-1]):
         solo = _fresh([r])
-        serving.ServingEngine(group_steps=5).run(solo)
+        _engine(kind, group_steps=5).run(solo)
         assert torch.equal(solo[0].out, r.out)
         assert torch.equal(solo[0].out_normalized, r.out_normalized)
 
 
-def test_serving_matches_fused_fit(cuda):
+@pytest.mark.parametrize("kind", ["native", "python"])
+def test_serving_matches_fused_fit(cuda, kind):
     specs, meshes = _stream(n=3, seed=5)
     reqs = serving.requests_from_meshes(meshes, specs, device=cuda)
     src_before = [r.srcV.clone() for r in reqs]
-    serving.ServingEngine(group_steps=7).run(reqs)
+    _engine(kind, group_steps=7).run(reqs)
     for r, (Vs, Fs, Vt, Ft), v0 in zip(reqs, meshes, src_before):
         assert torch.equal(r.srcV, v0), "device-resident inputs must not be modified"
         pid = PD.InitializeDeformTemplate(torch.from_numpy(Vt), torch.from_numpy(Ft), 0, r.N)
@@ -65,14 +73,15 @@ def test_serving_matches_fused_fit(cuda):
         assert torch.equal(den.cpu(), r.out.cpu())
 
 
-def test_bad_request_is_isolated(cuda):
+@pytest.mark.parametrize("kind", ["native", "python"])
+def test_bad_request_is_isolated(cuda, kind):
     specs, meshes = _stream(n=4, seed=8)
     reqs = serving.requests_from_meshes(meshes, specs, device=None, pin=True)
     bad = reqs[1]
     F = bad.srcF.clone()
     F[0, 0] = 10 ** 7
     reqs[1] = serving.Request(bad.id, bad.srcV, F, bad.tarV, bad.tarF, N=bad.N, steps=bad.steps)
-    serving.ServingEngine(group_steps=8).run(reqs)
+    _engine(kind, group_steps=8).run(reqs)
     assert reqs[1].error is not None and reqs[1].out is None
     for i in (0, 2, 3):
         assert reqs[i].error is None and reqs[i].out is not None
