@@ -579,9 +579,11 @@ int mo_mlp_bwd(const float* gk, const float* u, int64_t n, const float* W1, cons
                const float* W4, const float* store, int64_t astride, float* gz3, float* gz2, float* gu,
                float* partial, void* stream);
 /* dW4 [3,M], db4 [3], db3, db2, db1 [M], dW1 [M,3] += the sums of `rows`
- * partial rows, in row order. */
-int mo_mlp_partial_reduce(const float* partial, int64_t rows, float* dW4, float* db4, float* db3, float* db2,
-                          float* db1, float* dW1, void* stream);
+ * partial rows (summed in groups of consecutive rows, then the groups in
+ * order: deterministic).  scratch: mo_mlp_partial_reduce_bytes(). */
+size_t mo_mlp_partial_reduce_bytes(void);
+int mo_mlp_partial_reduce(const float* partial, int64_t rows, float* scratch, float* dW4, float* db4, float* db3,
+                          float* db2, float* db1, float* dW1, void* stream);
 /* dW [M,M] += A^T B (A, B [rows,M]: dW[o][i] = sum_r A[r][o] B[r][i]),
  * split over rows into `splits` partial sums (partial:
  * mo_mlp_wgrad_partial_bytes(splits)) added in split order. */

@@ -128,7 +128,8 @@ _SIGS = {
     "mo_mlp_transpose": (_I, [_P, _P, _P]),
     "mo_mlp_fwd": (_I, [_P, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _F, _F, _I, _P, _P, _P, _I64, _P]),
     "mo_mlp_bwd": (_I, [_P, _P, _I64, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _P]),
-    "mo_mlp_partial_reduce": (_I, [_P, _I64, _P, _P, _P, _P, _P, _P, _P]),
+    "mo_mlp_partial_reduce_bytes": (_SZ, []),
+    "mo_mlp_partial_reduce": (_I, [_P, _I64, _P, _P, _P, _P, _P, _P, _P, _P]),
     "mo_mlp_wgrad_partial_bytes": (_SZ, [_I]),
     "mo_mlp_wgrad": (_I, [_P, _P, _I64, _I, _P, _P, _P]),
     "mo_pack_pos": (_I, [_P, _I64, _P, _P]),

@@ -440,14 +440,28 @@ __global__ void __launch_bounds__(THREADS, 2)
     }
 }
 
-// out[p] += sum over rows t (in order) of partial[t][p]: the small gradients.
-__global__ void k_mlp_partial_reduce(const float* __restrict__ partial, int64_t rows, float* __restrict__ dW4,
+// The small gradients, in two passes with a fixed order: pass 1 sums the
+// rows of group blockIdx.y into mid[blockIdx.y][p]; pass 2 adds the groups'
+// sums, in group order, into the gradients.
+constexpr int RED_GROUPS = 128;
+__global__ void k_mlp_partial_sum(const float* __restrict__ partial, int64_t rows, int64_t rows_per_group,
+                                  float* __restrict__ mid) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= PW) return;
+    const int64_t t0 = (int64_t)blockIdx.y * rows_per_group;
+    const int64_t t1 = min(rows, t0 + rows_per_group);
+    float s = 0.f;
+    for (int64_t t = t0; t < t1; ++t) s += partial[t * PW + p];
+    mid[(int64_t)blockIdx.y * PW + p] = s;
+}
+
+__global__ void k_mlp_partial_reduce(const float* __restrict__ mid, int groups, float* __restrict__ dW4,
                                      float* __restrict__ db4, float* __restrict__ db3, float* __restrict__ db2,
                                      float* __restrict__ db1, float* __restrict__ dW1) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= PW) return;
     float s = 0.f;
-    for (int64_t t = 0; t < rows; ++t) s += partial[t * PW + p];
+    for (int g = 0; g < groups; ++g) s += mid[(int64_t)g * PW + p];
     if (p < P_DB4) {
         dW4[p] += s;  // [3][M] as stored
     } else if (p < P_DB3) {
@@ -617,13 +631,20 @@ extern "C" int mo_mlp_bwd(const float* gk, const float* u, int64_t n, const floa
     return MO_OK;
 }
 
-extern "C" int mo_mlp_partial_reduce(const float* partial, int64_t rows, float* dW4, float* db4, float* db3,
-                                     float* db2, float* db1, float* dW1, void* stream) {
+extern "C" size_t mo_mlp_partial_reduce_bytes(void) { return (size_t)RED_GROUPS * PW * sizeof(float); }
+
+extern "C" int mo_mlp_partial_reduce(const float* partial, int64_t rows, float* scratch, float* dW4, float* db4,
+                                     float* db3, float* db2, float* db1, float* dW1, void* stream) {
     MO_CHECK_ARG(rows >= 0, "negative row count");
     if (rows == 0) return MO_OK;
-    MO_CHECK_ARG(partial && dW4 && db4 && db3 && db2 && db1 && dW1, "null pointer");
-    k_mlp_partial_reduce<<<ceil_div(PW, 256), 256, 0, as_stream(stream)>>>(partial, rows, dW4, db4, db3, db2, db1,
-                                                                          dW1);
+    MO_CHECK_ARG(partial && scratch && dW4 && db4 && db3 && db2 && db1 && dW1, "null pointer");
+    const int64_t per = (rows + RED_GROUPS - 1) / RED_GROUPS;
+    const int groups = (int)((rows + per - 1) / per);
+    cudaStream_t s = as_stream(stream);
+    k_mlp_partial_sum<<<dim3(ceil_div(PW, 128), groups), 128, 0, s>>>(partial, rows, per, scratch);
+    ::mo::note_launch();
+    MO_LAUNCH_CHECK("k_mlp_partial_sum");
+    k_mlp_partial_reduce<<<ceil_div(PW, 256), 256, 0, s>>>(scratch, groups, dW4, db4, db3, db2, db1, dW1);
     ::mo::note_launch();
     MO_LAUNCH_CHECK("k_mlp_partial_reduce");
     return MO_OK;

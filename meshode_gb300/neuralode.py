@@ -152,6 +152,7 @@ class _Backward:
         self.wpart = torch.empty(int(lib.mo_mlp_wgrad_partial_bytes(self.splits)) // 4, dtype=torch.float32,
                                  device=dev)
         self.gu = [torch.empty(n, 3, dtype=torch.float32, device=dev) for _ in range(4)]
+        self.red = torch.empty(int(lib.mo_mlp_partial_reduce_bytes()) // 4, dtype=torch.float32, device=dev)
 
     def stage_vjp(self, P, st, s, u, gk):
         """dL/du of evaluation s (0..3) of the step for dL/dk = gk."""
@@ -169,8 +170,8 @@ class _Backward:
         n, M = self.n, self.M
         dW1, db1, dW2, db2, dW3, db3, dW4, db4 = grads
         s = stream_ptr()
-        call("mo_mlp_partial_reduce", ptr(self.partial), 4 * self.tiles * 8, ptr(dW4), ptr(db4), ptr(db3),
-             ptr(db2), ptr(db1), ptr(dW1), s)
+        call("mo_mlp_partial_reduce", ptr(self.partial), 4 * self.tiles * 8, ptr(self.red), ptr(dW4), ptr(db4),
+             ptr(db3), ptr(db2), ptr(db1), ptr(dW1), s)
         call("mo_mlp_wgrad", ptr(self.gz), ptr(st.array(3)), 4 * n, self.splits, ptr(self.wpart), ptr(dW3), s)
         call("mo_mlp_wgrad", ptr(self.gz[4 * n * M:]), ptr(st.array(1)), 4 * n, self.splits, ptr(self.wpart),
              ptr(dW2), s)
