@@ -104,24 +104,37 @@ __device__ __forceinline__ float dotf3(float3 a, float x, float y, float z) {
     return fmaf(a.z, z, fmaf(a.y, y, __fmul_rn(a.x, x)));
 }
 
-// Traversal record of an internal node: NODE_F4 float4, per child (left,
-// then right) (o.xyz, e.x) (a1.xyz, e.y) (a2.xyz, e.z) (a3.xyz, id), then
-// (left count, right count, 0, 0) as ints.  o: the box's origin corner,
-// a1..a3 its axes (a3 = obb_a3(a1, a2), stored so the walk does not
-// recompute it), e its extents; id >= 0 an internal node, ~first for a
-// bucket of `count` (1..DF_BUCKET) sorted triangles (count 0: internal).
+// Traversal record of an internal node: NODE_F4 float4 holding both
+// children's oriented boxes interleaved, each float2 (left, right), so that
+// one packed FP32 pass (FFMA2 / FADD2) bounds both children:
+//   w0 = (-o.x, -o.y)  w1 = (-o.z, -e.x)  w2 = (a1.x, a1.y)  w3 = (a1.z, -e.y)
+//   w4 = (a2.x, a2.y)  w5 = (a2.z, -e.z)  w6 = (a3.x, a3.y)  w7 = (a3.z, id)
+//   w8 = (left count, right count, 0, 0) as ints
+// where each named component is a (left, right) pair: w0 = (-oL.x, -oR.x,
+// -oL.y, -oR.y) and so on.  o: a box's origin corner, a1..a3 its axes
+// (a3 = obb_a3(a1, a2), stored so the walk does not recompute it), e its
+// extents (origin and extents stored negated: the walk adds them); id >= 0
+// an internal node, ~first for a bucket of `count` (1..DF_BUCKET) sorted
+// triangles (count 0: internal).
 constexpr int NODE_F4 = 9;
 
-// Squared distance from p to a child's box (the bound the traversal uses).
-__device__ __forceinline__ float obb_d2(float px, float py, float pz, float4 g0, float4 g1, float4 g2, float4 g3) {
-    const float qx = __fsub_rn(px, g0.x), qy = __fsub_rn(py, g0.y), qz = __fsub_rn(pz, g0.z);
-    const float3 a1 = make_float3(g1.x, g1.y, g1.z), a2 = make_float3(g2.x, g2.y, g2.z);
-    const float3 a3 = make_float3(g3.x, g3.y, g3.z);
-    const float t1 = dotf3(a1, qx, qy, qz), t2 = dotf3(a2, qx, qy, qz), t3 = dotf3(a3, qx, qy, qz);
-    const float s1 = fmaxf(fmaxf(-t1, t1 - g0.w), 0.f);
-    const float s2 = fmaxf(fmaxf(-t2, t2 - g1.w), 0.f);
-    const float s3 = fmaxf(fmaxf(-t3, t3 - g2.w), 0.f);
-    return s1 * s1 + s2 * s2 + s3 * s3;
+__device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
+
+// Squared distances from p (broadcast in Px, Py, Pz) to the left and right
+// child's boxes of a record: the bound the traversal uses, both children in
+// one packed pass (each half the one-box arithmetic in the same order).
+__device__ __forceinline__ float2 obb_pair_d2(float2 Px, float2 Py, float2 Pz, float4 w0, float4 w1, float4 w2,
+                                              float4 w3, float4 w4, float4 w5, float4 w6, float4 w7) {
+    const float2 qx = __fadd2_rn(Px, lo2(w0)), qy = __fadd2_rn(Py, hi2(w0)), qz = __fadd2_rn(Pz, lo2(w1));
+    const float2 t1 = __ffma2_rn(lo2(w3), qz, __ffma2_rn(hi2(w2), qy, __fmul2_rn(lo2(w2), qx)));
+    const float2 t2 = __ffma2_rn(lo2(w5), qz, __ffma2_rn(hi2(w4), qy, __fmul2_rn(lo2(w4), qx)));
+    const float2 t3 = __ffma2_rn(lo2(w7), qz, __ffma2_rn(hi2(w6), qy, __fmul2_rn(lo2(w6), qx)));
+    const float2 u1 = __fadd2_rn(t1, hi2(w1)), u2 = __fadd2_rn(t2, hi2(w3)), u3 = __fadd2_rn(t3, hi2(w5));
+    const float2 s1 = make_float2(fmaxf(fmaxf(-t1.x, u1.x), 0.f), fmaxf(fmaxf(-t1.y, u1.y), 0.f));
+    const float2 s2 = make_float2(fmaxf(fmaxf(-t2.x, u2.x), 0.f), fmaxf(fmaxf(-t2.y, u2.y), 0.f));
+    const float2 s3 = make_float2(fmaxf(fmaxf(-t3.x, u3.x), 0.f), fmaxf(fmaxf(-t3.y, u3.y), 0.f));
+    return __ffma2_rn(s3, s3, __ffma2_rn(s2, s2, __fmul2_rn(s1, s1)));
 }
 
 // ---------------------------------------------------------------------------
@@ -285,15 +298,26 @@ __device__ __forceinline__ float2 tri_d2_t2(float px, float py, float pz, const 
     return make_float2(ina ? h2.x : hd.x, inb ? h2.y : hd.y);
 }
 
-// obb_d2 for two points (a bound only: its rounding may differ from the
-// one-point form by a few ulps, far inside the traversal's slack).
-__device__ __forceinline__ float2 obb_d2_2(float2 px, float2 py, float2 pz, float4 g0, float4 g1, float4 g2,
-                                           float4 g3) {
-    const float2 qx = __fadd2_rn(px, bc2(-g0.x)), qy = __fadd2_rn(py, bc2(-g0.y)), qz = __fadd2_rn(pz, bc2(-g0.z));
-    const float2 t1 = dot3e2(qx, qy, qz, g1.x, g1.y, g1.z);
-    const float2 t2 = dot3e2(qx, qy, qz, g2.x, g2.y, g2.z);
-    const float2 t3 = dot3e2(qx, qy, qz, g3.x, g3.y, g3.z);
-    const float2 u1 = __fadd2_rn(t1, bc2(-g0.w)), u2 = __fadd2_rn(t2, bc2(-g1.w)), u3 = __fadd2_rn(t3, bc2(-g2.w));
+// Component SIDE (0: left, 1: right) of the low (x, y) or high (z, w) pair
+// of a record word.
+template <int SIDE>
+__device__ __forceinline__ float sel(float4 v, bool hi) {
+    return hi ? (SIDE ? v.w : v.z) : (SIDE ? v.y : v.x);
+}
+
+// The box distance of one child (SIDE) of a record for two points (a bound
+// only: its rounding may differ from the one-point form by a few ulps, far
+// inside the traversal's slack).
+template <int SIDE>
+__device__ __forceinline__ float2 obb_d2_2(float2 px, float2 py, float2 pz, float4 w0, float4 w1, float4 w2,
+                                           float4 w3, float4 w4, float4 w5, float4 w6, float4 w7) {
+    const float2 qx = __fadd2_rn(px, bc2(sel<SIDE>(w0, false))), qy = __fadd2_rn(py, bc2(sel<SIDE>(w0, true))),
+                 qz = __fadd2_rn(pz, bc2(sel<SIDE>(w1, false)));
+    const float2 t1 = dot3e2(qx, qy, qz, sel<SIDE>(w2, false), sel<SIDE>(w2, true), sel<SIDE>(w3, false));
+    const float2 t2 = dot3e2(qx, qy, qz, sel<SIDE>(w4, false), sel<SIDE>(w4, true), sel<SIDE>(w5, false));
+    const float2 t3 = dot3e2(qx, qy, qz, sel<SIDE>(w6, false), sel<SIDE>(w6, true), sel<SIDE>(w7, false));
+    const float2 u1 = __fadd2_rn(t1, bc2(sel<SIDE>(w1, true))), u2 = __fadd2_rn(t2, bc2(sel<SIDE>(w3, true))),
+                 u3 = __fadd2_rn(t3, bc2(sel<SIDE>(w5, true)));
     const float2 s1 = make_float2(fmaxf(fmaxf(-t1.x, u1.x), 0.f), fmaxf(fmaxf(-t1.y, u1.y), 0.f));
     const float2 s2 = make_float2(fmaxf(fmaxf(-t2.x, u2.x), 0.f), fmaxf(fmaxf(-t2.y, u2.y), 0.f));
     const float2 s3 = make_float2(fmaxf(fmaxf(-t3.x, u3.x), 0.f), fmaxf(fmaxf(-t3.y, u3.y), 0.f));
@@ -330,6 +354,7 @@ __device__ __forceinline__ float df_voxel_value(const float4* __restrict__ nodes
     // every distance below it.
     float lim = valid ? (init == FLT_MAX ? FLT_MAX : slack_bound(init)) : -1.0f;
     const unsigned FULL = 0xffffffffu;
+    const float2 P2x = make_float2(px, px), P2y = make_float2(py, py), P2z = make_float2(pz, pz);
     unsigned long long n_visit = 0, n_test = 0;  // warp-uniform (COUNT only)
     if (ntri == 1) {
         const float t = tri_d2(px, py, pz, load_tri(tris, 0), best);
@@ -348,12 +373,13 @@ __device__ __forceinline__ float df_voxel_value(const float4* __restrict__ nodes
             }
             if (COUNT) ++n_visit;
             const float4* nd = nodes + NODE_F4 * (int64_t)node;
-            const float4 l0 = __ldg(nd), l1 = __ldg(nd + 1), l2 = __ldg(nd + 2), l3 = __ldg(nd + 3);
-            const float4 r0 = __ldg(nd + 4), r1 = __ldg(nd + 5), r2 = __ldg(nd + 6), r3 = __ldg(nd + 7);
+            const float4 w0 = __ldg(nd), w1 = __ldg(nd + 1), w2 = __ldg(nd + 2), w3 = __ldg(nd + 3);
+            const float4 w4 = __ldg(nd + 4), w5 = __ldg(nd + 5), w6 = __ldg(nd + 6), w7 = __ldg(nd + 7);
             const int2 cnt = __ldg(reinterpret_cast<const int2*>(nd + 8));
-            const int L = __float_as_int(l3.w), R = __float_as_int(r3.w);
+            const int L = __float_as_int(w7.z), R = __float_as_int(w7.w);
             const int cl = cnt.x, cr = cnt.y;  // bucket sizes (0: internal)
-            const float dl = obb_d2(px, py, pz, l0, l1, l2, l3), dr = obb_d2(px, py, pz, r0, r1, r2, r3);
+            const float2 dlr = obb_pair_d2(P2x, P2y, P2z, w0, w1, w2, w3, w4, w5, w6, w7);
+            const float dl = dlr.x, dr = dlr.y;
             bool wl = __any_sync(FULL, dl < lim);
             bool wr = __any_sync(FULL, dr < lim);
             // the opened buckets' triangles, left then right, one test body
@@ -459,12 +485,13 @@ __device__ __forceinline__ float2 df_voxel_value2(const float4* __restrict__ nod
             }
             if (COUNT) ++n_visit;
             const float4* nd = nodes + NODE_F4 * (int64_t)node;
-            const float4 l0 = __ldg(nd), l1 = __ldg(nd + 1), l2 = __ldg(nd + 2), l3 = __ldg(nd + 3);
-            const float4 r0 = __ldg(nd + 4), r1 = __ldg(nd + 5), r2 = __ldg(nd + 6), r3 = __ldg(nd + 7);
+            const float4 w0 = __ldg(nd), w1 = __ldg(nd + 1), w2 = __ldg(nd + 2), w3 = __ldg(nd + 3);
+            const float4 w4 = __ldg(nd + 4), w5 = __ldg(nd + 5), w6 = __ldg(nd + 6), w7 = __ldg(nd + 7);
             const int2 cnt = __ldg(reinterpret_cast<const int2*>(nd + 8));
-            const int L = __float_as_int(l3.w), R = __float_as_int(r3.w);
+            const int L = __float_as_int(w7.z), R = __float_as_int(w7.w);
             const int cl = cnt.x, cr = cnt.y;
-            const float2 dl = obb_d2_2(px, py, pz, l0, l1, l2, l3), dr = obb_d2_2(px, py, pz, r0, r1, r2, r3);
+            const float2 dl = obb_d2_2<0>(px, py, pz, w0, w1, w2, w3, w4, w5, w6, w7);
+            const float2 dr = obb_d2_2<1>(px, py, pz, w0, w1, w2, w3, w4, w5, w6, w7);
             bool wl = __any_sync(FULL, dl.x < lim.x || dl.y < lim.y);
             bool wr = __any_sync(FULL, dr.x < lim.x || dr.y < lim.y);
             const int nl = wl ? cl : 0, nr = wr ? cr : 0;

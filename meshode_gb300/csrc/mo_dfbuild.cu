@@ -529,7 +529,9 @@ __global__ void k_obb_nodes(const float4* __restrict__ nodes, const int2* __rest
     // a node of at most DF_BUCKET triangles other than the root is never
     // visited (it is its parent's bucket, or inside one)
     if (i != 0 && range[i].y - range[i].x + 1 <= DF_BUCKET) return;
-    int cnts[2];
+    int cnts[2], ids[2];
+    Obb bs[2];
+    float3 a3s[2];
     for (int side = 0; side < 2; ++side) {
         const int c = __float_as_int(nodes[4 * (int64_t)i + side].w);
         int id = c, cnt = 0;
@@ -546,15 +548,25 @@ __global__ void k_obb_nodes(const float4* __restrict__ nodes, const int2* __rest
                 cnt = r.y - r.x + 1;
             }
         }
-        const float3 a3 = obb_a3(b.a1, b.a2);
-        float4* t = tnodes + NODE_F4 * (int64_t)i + 4 * side;
-        t[0] = make_float4(b.o.x, b.o.y, b.o.z, b.e.x);
-        t[1] = make_float4(b.a1.x, b.a1.y, b.a1.z, b.e.y);
-        t[2] = make_float4(b.a2.x, b.a2.y, b.a2.z, b.e.z);
-        t[3] = make_float4(a3.x, a3.y, a3.z, __int_as_float(id));
+        bs[side] = b;
+        a3s[side] = obb_a3(b.a1, b.a2);
+        ids[side] = id;
         cnts[side] = cnt;
     }
-    tnodes[NODE_F4 * (int64_t)i + 8] = make_float4(__int_as_float(cnts[0]), __int_as_float(cnts[1]), 0.f, 0.f);
+    // the two children interleaved (left, right) per float2, origin and
+    // extents negated (see NODE_F4)
+    const Obb& L = bs[0];
+    const Obb& R = bs[1];
+    float4* t = tnodes + NODE_F4 * (int64_t)i;
+    t[0] = make_float4(-L.o.x, -R.o.x, -L.o.y, -R.o.y);
+    t[1] = make_float4(-L.o.z, -R.o.z, -L.e.x, -R.e.x);
+    t[2] = make_float4(L.a1.x, R.a1.x, L.a1.y, R.a1.y);
+    t[3] = make_float4(L.a1.z, R.a1.z, -L.e.y, -R.e.y);
+    t[4] = make_float4(L.a2.x, R.a2.x, L.a2.y, R.a2.y);
+    t[5] = make_float4(L.a2.z, R.a2.z, -L.e.z, -R.e.z);
+    t[6] = make_float4(a3s[0].x, a3s[1].x, a3s[0].y, a3s[1].y);
+    t[7] = make_float4(a3s[0].z, a3s[1].z, __int_as_float(ids[0]), __int_as_float(ids[1]));
+    t[8] = make_float4(__int_as_float(cnts[0]), __int_as_float(cnts[1]), 0.f, 0.f);
 }
 
 // The full grid: one warp per packet of PX x PY x PZ voxels.
