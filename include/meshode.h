@@ -267,6 +267,10 @@ int mo_edge_backward_w(const float* V, int64_t nv, const void* csr, int64_t nh, 
 int mo_sell_plan(const void* csr, int64_t nv, int64_t nh, int32_t* slice_ptr, void* stream);
 int mo_sell_fill(const void* csr, int64_t nv, int64_t nh, const int32_t* slice_ptr, int32_t* records,
                  void* stream);
+/* Per-edge weights w [H] laid out like the records (record_w: as many floats
+ * as records; padding 0), for the weighted fused step (MoPair.sell_w). */
+int mo_sell_fill_w(const void* csr, int64_t nv, int64_t nh, const int32_t* slice_ptr, const float* w,
+                   float* record_w, void* stream);
 
 /* ------------------------------------------------------------------------
  * Adam.  Replaces torch.optim.Adam([V], lr) in the reference's loops
@@ -329,6 +333,12 @@ typedef struct MoPair {
     int32_t df_queue_cap;
     float df_band;             /* the build band (mo_df_loss_band(N)) */
     int32_t df_pad;
+    /* Per-edge weights (CadEdgeLoss, src/interface/cad_layer.cc:152-223),
+     * read only by mo_fused_step_weighted: mo_sell_fill_w's record-aligned
+     * copy; NULL there means weight 1.  Each record contributes
+     * (v1 - v0 - off) * w^2 to the gradient and ((v1 - v0 - off) * w)^2 to
+     * the energy. */
+    const float* sell_w;
 } MoPair;
 
 typedef struct MoTile {
@@ -346,6 +356,13 @@ typedef struct MoTile {
 #define MO_TILE_WARPS 8
 int mo_fused_step(const MoPair* pairs, const MoTile* tiles, const int32_t* ntiles, int max_tiles,
                   int launch_index, float* tile_loss, int grid_ctas, void* stream);
+/* mo_fused_step for pairs with per-edge weights (MoPair.sell_w): the
+ * CadLossFunction objective (src/python/layers/cad_loss_layer.py:9-31,
+ * cad_layer.cc:79-223) -- 0.5 sum d^2 + w_edge * 0.5 sum |r * w_e|^2 -- and
+ * its gradient in the serial-scatter order.  A separate instantiation, so
+ * the unweighted kernel carries no weight loads. */
+int mo_fused_step_weighted(const MoPair* pairs, const MoTile* tiles, const int32_t* ntiles, int max_tiles,
+                           int launch_index, float* tile_loss, int grid_ctas, void* stream);
 /* mo_fused_step for pairs with on-demand grids (df_cells set): also queues
  * the cells the step moves vertices into (see MoPair). */
 int mo_fused_step_on_demand(const MoPair* pairs, const MoTile* tiles, const int32_t* ntiles, int max_tiles,

@@ -40,7 +40,7 @@ class MoPair(ctypes.Structure):
         ("t0", ctypes.c_int32), ("t_end", ctypes.c_int32), ("tile0", ctypes.c_int32), ("ntiles", ctypes.c_int32),
         ("df_tree", _P), ("df_lin", _P), ("df_cells", _P), ("df_packets", _P), ("df_status", _P),
         ("df_queue", _P), ("df_pqueue", _P), ("df_queue_count", _P), ("df_ntri", ctypes.c_int32), ("df_queue_cap", ctypes.c_int32),
-        ("df_band", _F), ("df_pad", ctypes.c_int32),
+        ("df_band", _F), ("df_pad", ctypes.c_int32), ("sell_w", _P),
     ]
 
 
@@ -117,8 +117,10 @@ _SIGS = {
     "mo_edge_backward_w": (_I, [_P, _I64, _P, _I64, _P, _P, _P, _P]),
     "mo_sell_plan": (_I, [_P, _I64, _I64, _P, _P]),
     "mo_sell_fill": (_I, [_P, _I64, _I64, _P, _P, _P]),
+    "mo_sell_fill_w": (_I, [_P, _I64, _I64, _P, _P, _P, _P]),
     "mo_adam_step": (_I, [_P, _P, _P, _P, _I64, _F, _F, _F, _F, _F, _F, _P]),
     "mo_fused_step": (_I, [_P, _P, _P, _I, _I, _P, _I, _P]),
+    "mo_fused_step_weighted": (_I, [_P, _P, _P, _I, _I, _P, _I, _P]),
     "mo_fused_step_on_demand": (_I, [_P, _P, _P, _I, _I, _P, _I, _P]),
     "mo_pair_loss": (_I, [_P, _I, _I, _I, _P, _P, _P]),
     "mo_abi_sizes": (_I, [ctypes.POINTER(_SZ), ctypes.POINTER(_SZ)]),

@@ -306,6 +306,23 @@ __global__ void k_sell_fill(int64_t nv, int64_t nslices, const int* __restrict__
         rec[base + (int64_t)k * 32 + lane] = (k < deg) ? (other[b + k] | ((key[b + k] & 1) << 31)) : -1;
 }
 
+// The weight of every sliced-ELL record (w[h] of the record's half-edge h),
+// in the records' layout; padding 0.
+__global__ void k_sell_fill_w(int64_t nv, int64_t nslices, const int* __restrict__ row_ptr,
+                              const int* __restrict__ key, const int* __restrict__ slice_ptr,
+                              const float* __restrict__ w, float* __restrict__ rec_w) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t s = t >> 5;
+    const int lane = threadIdx.x & 31;
+    if (s >= nslices) return;
+    const int64_t v = s * 32 + lane;
+    const int base = slice_ptr[s];
+    const int width = (slice_ptr[s + 1] - base) >> 5;
+    const int b = v < nv ? row_ptr[v] : 0;
+    const int deg = v < nv ? row_ptr[v + 1] - b : 0;
+    for (int k = 0; k < width; ++k) rec_w[base + (int64_t)k * 32 + lane] = (k < deg) ? w[key[b + k] >> 1] : 0.f;
+}
+
 }  // namespace mo
 
 using namespace mo;
@@ -481,5 +498,19 @@ extern "C" int mo_sell_fill(const void* csr, int64_t nv, int64_t nh, const int32
     k_sell_fill<<<ceil_div(nslices * 32, 256), 256, 0, as_stream(stream)>>>(nv, nslices, c.row_ptr, c.key, c.other,
                                                                            slice_ptr, records); ::mo::note_launch();
     MO_LAUNCH_CHECK("k_sell_fill");
+    return MO_OK;
+}
+
+extern "C" int mo_sell_fill_w(const void* csr, int64_t nv, int64_t nh, const int32_t* slice_ptr, const float* w,
+                              float* record_w, void* stream) {
+    MO_CHECK_ARG(nv >= 0 && nh >= 0, "negative size");
+    if (nv == 0) return MO_OK;
+    MO_CHECK_ARG(csr && slice_ptr && w && record_w, "null pointer");
+    const int64_t nslices = (nv + 31) / 32;
+    CsrView c = csr_view(const_cast<void*>(csr), nv, nh);
+    k_sell_fill_w<<<ceil_div(nslices * 32, 256), 256, 0, as_stream(stream)>>>(nv, nslices, c.row_ptr, c.key,
+                                                                             slice_ptr, w, record_w);
+    ::mo::note_launch();
+    MO_LAUNCH_CHECK("k_sell_fill_w");
     return MO_OK;
 }

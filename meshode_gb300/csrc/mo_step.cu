@@ -47,8 +47,10 @@ __device__ __forceinline__ DFJet df_eval_layout(const float* grid, int N, float 
 // other warps of its block.  ON_DEMAND: the pairs' grids are filled on
 // demand, and a vertex moving into a cell not yet filled queues it (a
 // separate instantiation: the queueing code slows the plain kernel down even
-// when it is skipped).
-template <bool ON_DEMAND>
+// when it is skipped).  WEIGHTED: every record carries a weight
+// (MoPair.sell_w, NULL: 1): the gradient takes r * w^2 and the energy
+// (r * w)^2 (CadEdgeLoss), another separate instantiation.
+template <bool ON_DEMAND, bool WEIGHTED = false>
 __global__ void __launch_bounds__(STEP_THREADS, 4) k_fused_step(const MoPair* __restrict__ pairs,
                                                              const MoTile* __restrict__ tiles,
                                                              const int* __restrict__ ntiles_p, int max_tiles,
@@ -88,6 +90,7 @@ __global__ void __launch_bounds__(STEP_THREADS, 4) k_fused_step(const MoPair* __
         int c[REC_UNROLL];
 #pragma unroll
         for (int u = 0; u < REC_UNROLL; ++u) c[u] = (u < rows) ? __ldg(rec + u * 32) : -1;
+        const float* __restrict__ recw = WEIGHTED && P.sell_w ? P.sell_w + rb + lane : nullptr;
         const int N = P.N;
         const float Nf = (float)N, Cf = (float)((double)(N - 1) - 1e-3);
         const DFJet j = (P.layout == MO_LAYOUT_CELL)
@@ -135,10 +138,24 @@ __global__ void __launch_bounds__(STEP_THREADS, 4) k_fused_step(const MoPair* __
                 const float rx = SUB(SUB(q[u].x, p.x), SUB(sr[u].x, r0.x));
                 const float ry = SUB(SUB(q[u].y, p.y), SUB(sr[u].y, r0.y));
                 const float rz = SUB(SUB(q[u].z, p.z), SUB(sr[u].z, r0.z));
-                if (c[u] != -1) {
-                    grx = SUB(grx, rx); gry = SUB(gry, ry); grz = SUB(grz, rz);
+                if (WEIGHTED) {
+                    // (v1 - v0 - off) * (w * w) as cad_layer.cc:195-202
+                    // rounds it; the v1 role's r is the v0 role's negated
+                    const float we_ = (recw && c[u] != -1) ? __ldg(recw + (row + u) * 32) : 1.0f;
+                    const float l2 = MUL(we_, we_);
+                    if (c[u] != -1) {
+                        grx = SUB(grx, MUL(rx, l2)); gry = SUB(gry, MUL(ry, l2)); grz = SUB(grz, MUL(rz, l2));
+                    }
+                    if (c[u] >= 0) {
+                        const float ex = MUL(rx, we_), ey = MUL(ry, we_), ez = MUL(rz, we_);
+                        esq += ex * ex + ey * ey + ez * ez;
+                    }
+                } else {
+                    if (c[u] != -1) {
+                        grx = SUB(grx, rx); gry = SUB(gry, ry); grz = SUB(grz, rz);
+                    }
+                    if (c[u] >= 0) esq += rx * rx + ry * ry + rz * rz;
                 }
-                if (c[u] >= 0) esq += rx * rx + ry * ry + rz * rz;
             }
             if (c[REC_UNROLL - 1] == -1) break;
 #pragma unroll
@@ -241,16 +258,19 @@ extern "C" int mo_adam_step(float* P, const float* G, float* M, float* Vsq, int6
     return MO_OK;
 }
 
-static int launch_fused_step(bool on_demand, const MoPair* pairs, const MoTile* tiles, const int32_t* ntiles,
+static int launch_fused_step(int variant, const MoPair* pairs, const MoTile* tiles, const int32_t* ntiles,
                              int max_tiles, int launch_index, float* tile_loss, int grid_ctas, void* stream) {
     MO_CHECK_ARG(pairs && tiles && ntiles && tile_loss, "null pointer");
     MO_CHECK_ARG(max_tiles >= 0 && launch_index >= 0, "negative size");
     if (max_tiles == 0) return MO_OK;
     int ctas = grid_ctas > 0 ? grid_ctas : step_ctas();
     if (ctas > max_tiles) ctas = max_tiles;
-    if (on_demand)
+    if (variant == 1)
         k_fused_step<true><<<ctas, STEP_THREADS, 0, as_stream(stream)>>>(pairs, tiles, ntiles, max_tiles,
                                                                          launch_index, tile_loss);
+    else if (variant == 2)
+        k_fused_step<false, true><<<ctas, STEP_THREADS, 0, as_stream(stream)>>>(pairs, tiles, ntiles, max_tiles,
+                                                                                launch_index, tile_loss);
     else
         k_fused_step<false><<<ctas, STEP_THREADS, 0, as_stream(stream)>>>(pairs, tiles, ntiles, max_tiles,
                                                                           launch_index, tile_loss);
@@ -261,13 +281,18 @@ static int launch_fused_step(bool on_demand, const MoPair* pairs, const MoTile* 
 
 extern "C" int mo_fused_step(const MoPair* pairs, const MoTile* tiles, const int32_t* ntiles, int max_tiles,
                              int launch_index, float* tile_loss, int grid_ctas, void* stream) {
-    return launch_fused_step(false, pairs, tiles, ntiles, max_tiles, launch_index, tile_loss, grid_ctas, stream);
+    return launch_fused_step(0, pairs, tiles, ntiles, max_tiles, launch_index, tile_loss, grid_ctas, stream);
+}
+
+extern "C" int mo_fused_step_weighted(const MoPair* pairs, const MoTile* tiles, const int32_t* ntiles, int max_tiles,
+                                      int launch_index, float* tile_loss, int grid_ctas, void* stream) {
+    return launch_fused_step(2, pairs, tiles, ntiles, max_tiles, launch_index, tile_loss, grid_ctas, stream);
 }
 
 extern "C" int mo_fused_step_on_demand(const MoPair* pairs, const MoTile* tiles, const int32_t* ntiles,
                                        int max_tiles, int launch_index, float* tile_loss, int grid_ctas,
                                        void* stream) {
-    return launch_fused_step(true, pairs, tiles, ntiles, max_tiles, launch_index, tile_loss, grid_ctas, stream);
+    return launch_fused_step(1, pairs, tiles, ntiles, max_tiles, launch_index, tile_loss, grid_ctas, stream);
 }
 
 extern "C" int mo_pair_loss(const MoPair* pairs, int npairs, int max_tiles, int nlaunch, const float* tile_loss,

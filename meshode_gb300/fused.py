@@ -52,12 +52,14 @@ class Pair:
 
     def __init__(self, grid, N, layout, V, csr, nh, rest, steps, lr=1e-3, betas=(0.9, 0.999), eps=1e-8,
                  w_edge=1.0, mask_thresh=None, grad_scale=1.0, debug_grad=False, stream=None, slice_ptr=None,
-                 nrec=None, slices_per_tile=SLICES_PER_TILE):
+                 nrec=None, slices_per_tile=SLICES_PER_TILE, edge_w=None):
         """V: normalised source vertices, float32 [nv,3] on the device (the
         optimiser's start).  csr/nh: the edge CSR buffer and half-edge count.
         rest: float32 [nv,3] positions the rest offsets were taken from (the V
         given to StoreRigidityInformation).  When slice_ptr/nrec are given, the
-        sliced-ELL plan was already made."""
+        sliced-ELL plan was already made.  edge_w: optional float32 [nh]
+        per-edge weights (CadEdgeLoss); the pair then needs the weighted step
+        (StepGroupRunner(weighted=True))."""
         dev = V.device
         s = stream_ptr(stream)
         self.device = dev
@@ -93,6 +95,11 @@ class Pair:
         self.nrec = int(nrec)
         self.sell = torch.empty(max(self.nrec, 1), dtype=torch.int32, device=dev)
         call("mo_sell_fill", ptr(csr), self.nv, nh, ptr(self.slice_ptr), ptr(self.sell), s)
+        self.sell_w = None
+        if edge_w is not None:
+            self.sell_w = torch.empty(max(self.nrec, 1), dtype=torch.float32, device=dev)
+            call("mo_sell_fill_w", ptr(csr), self.nv, nh, ptr(self.slice_ptr), ptr(edge_w.contiguous()),
+                 ptr(self.sell_w), s)
         self.grad_dbg = torch.zeros(self.nv * 3, dtype=torch.float32, device=dev) if debug_grad else None
         self.adam_tab = adam_table(max(self.steps, 1), self.lr, self.b1, self.b2, dev)
         self.loss_history = []
@@ -145,6 +152,7 @@ class Pair:
         p.adam_v = self.v.data_ptr()
         p.adam_tab = self.adam_tab.data_ptr()
         p.grad_dbg = self.grad_dbg.data_ptr() if self.grad_dbg is not None else None
+        p.sell_w = self.sell_w.data_ptr() if self.sell_w is not None else None
         p.N, p.layout, p.nv, p.nslices = self.N, self.layout, self.nv, self.nslices
         p.w_edge = self.w_edge
         p.mask_thresh = float(self.mask_thresh) if self.mask_thresh is not None else 0.0
@@ -167,8 +175,9 @@ def tiles_for(nslices, slices_per_tile=SLICES_PER_TILE):
 class StepGroupRunner:
     """Runs groups of S fused steps over a set of pairs (graph-captured)."""
 
-    def __init__(self, device, max_pairs, max_tiles, group_steps=25, use_graph=True):
+    def __init__(self, device, max_pairs, max_tiles, group_steps=25, use_graph=True, weighted=False):
         self.device = device
+        self.weighted = bool(weighted)  # pairs with per-edge weights: mo_fused_step_weighted
         self.max_pairs = int(max_pairs)
         self.max_tiles = int(max_tiles)
         self.S = int(group_steps)
@@ -190,8 +199,9 @@ class StepGroupRunner:
 
     def _launch_group(self):
         s = stream_ptr()
+        step = "mo_fused_step_weighted" if self.weighted else "mo_fused_step"
         for k in range(self.S):
-            call("mo_fused_step", ptr(self.pairs_dev), ptr(self.tiles_dev), ptr(self.ntiles_dev), self.max_tiles, k,
+            call(step, ptr(self.pairs_dev), ptr(self.tiles_dev), ptr(self.ntiles_dev), self.max_tiles, k,
                  ptr(self.tile_loss), 0, s)
 
     def upload(self, pairs, t0s):
@@ -282,16 +292,19 @@ def pair_from_template(pid, src_V_norm, steps, lr=1e-3, w_edge=1.0, mask_thresh=
         raise RuntimeError("template %d has no stored edge information" % int(pid))
     V = src_V_norm.detach().to(p.device).contiguous()
     return Pair(p.grid, p.N, p.layout, V, st.csr, st.nh, st.rest, steps, lr=lr, w_edge=w_edge,
-                mask_thresh=mask_thresh, debug_grad=debug_grad, **kw)
+                mask_thresh=mask_thresh, debug_grad=debug_grad, edge_w=st.weights, **kw)
 
 
 def fused_fit(pid, src_V_norm, steps, lr=1e-3, group_steps=25, use_graph=True, w_edge=1.0, mask_thresh=None,
               record_loss=False):
     """Fit one pair with the fused step (the GPU-native form of the
-    reference's plain Adam loop, rigid_deform.py:34-41).  Returns
+    reference's plain Adam loop, rigid_deform.py:34-41; with the template's
+    CAD edges (StoreCadInformation), the CadLossFunction objective,
+    cad_loss_layer.py:9-31, on the weighted step).  Returns
     (final normalised positions [nv,3] on the device, per-step losses or None)."""
     pr = pair_from_template(pid, src_V_norm, steps, lr=lr, w_edge=w_edge, mask_thresh=mask_thresh)
-    runner = StepGroupRunner(pr.device, 1, pr.ntiles, group_steps=group_steps, use_graph=use_graph)
+    runner = StepGroupRunner(pr.device, 1, pr.ntiles, group_steps=group_steps, use_graph=use_graph,
+                             weighted=pr.sell_w is not None)
     losses = []
     while not pr.done:
         runner.upload([pr], [pr.t])

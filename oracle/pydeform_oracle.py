@@ -489,6 +489,19 @@ def graph_fit(src_V, src_E, pid, steps, rigidity2, lr=1e-3, adam="torch"):
     return V.detach()
 
 
+def cad_fit(src_V, src_F, src_E, pid, steps, lr=1e-3, adam="exact"):
+    """The CadLossFunction loop (src/python/layers/cad_loss_layer.py:9-31:
+    grad_h * (DistanceFieldLoss_backward + CadEdgeLoss_backward), grad_h = 1)
+    with Adam on the CPU (adam as in rigid_fit)."""
+    V = torch.nn.Parameter(src_V.clone())
+    opt = _optimizer(V, lr, adam)
+    for _ in range(steps):
+        with torch.no_grad():
+            g = 1.0 * (DistanceFieldLoss_backward(V.data, pid) + CadEdgeLoss_backward(V.data, src_F, src_E, pid))
+            _adam_step(opt, V, g)
+    return V.detach()
+
+
 def reverse_loss(src_V, tar_V):
     """ReverseLossLayer.forward (src/python/layers/reverse_loss_layer.py:14-25)
     on the CPU: cKDTree 1-NN of every target vertex among the source

@@ -126,3 +126,49 @@ def test_alone_vs_mix_bitexact(cuda, orc):
     # the third pair ran fewer steps: compare against its own alone run
     out3, _ = fused.fused_fit(built[2][0], built[2][2], K - 7, group_steps=5)
     assert torch.equal(prs[2].positions().cpu(), out3.cpu())
+
+
+def _cad_pair(cuda, orc, level=3, N=32, seed=4):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    V, F = meshgen.icosphere(level)
+    T = meshgen.displace(V, rng).astype(np.float32)
+    V = V.astype(np.float32)
+    F = F.astype(np.int32)
+    E = meshgen.edges_from_faces(F)[::3]
+    Tt, Ft, Et = torch.from_numpy(T), torch.from_numpy(F), torch.from_numpy(np.ascontiguousarray(E))
+    pid = PD.InitializeDeformTemplate(Tt, Ft, 0, N)
+    Vs = torch.from_numpy(V.copy())
+    PD.NormalizeByTemplate(Vs, pid)
+    PD.StoreCadInformation(Vs, Ft, Et, pid)
+    opid = orc.InitializeDeformTemplate(T, F, 0, N, grid=PD.GetDistanceField(pid).cpu().numpy())
+    orc.StoreCadInformation(Vs, Ft, Et, opid)
+    return pid, opid, Vs, Ft, Et
+
+
+def test_weighted_fused_step_bitexact_cad(cuda, orc):
+    """The weighted fused step (mo_fused_step_weighted: per-edge weights of
+    StoreCadInformation, E's edges then F's half-edges) against the oracle's
+    CadLossFunction loop (cad_loss_layer.py:9-31, cad_layer.cc:152-223) with
+    the op-by-op Adam: the first gradient and 30 steps bit for bit; the
+    unweighted step on the same pair differs (the weights are used)."""
+    pid, opid, Vs, F, E = _cad_pair(cuda, orc)
+    # start away from the rest pose, so that the edge residuals (and the
+    # weights) are not zero in the first step
+    rng = np.random.Generator(np.random.PCG64(12))
+    V0 = (Vs + torch.from_numpy(rng.normal(0, 0.01, Vs.shape).astype(np.float32))).contiguous()
+    pr = fused.pair_from_template(pid, V0, steps=1, debug_grad=True)
+    assert pr.sell_w is not None
+    runner = fused.StepGroupRunner(cuda, 1, pr.ntiles, group_steps=1, use_graph=False, weighted=True)
+    runner.upload([pr], [0])
+    runner.run_group()
+    g = pr.grad_dbg.view(-1, 3).cpu().numpy()
+    ref = (orc.DistanceFieldLoss_backward(V0, opid) + orc.CadEdgeLoss_backward(V0, F, E, opid)).numpy()
+    assert np.array_equal(g, ref), int((g != ref).sum())
+    out, _ = fused.fused_fit(pid, V0, 30, group_steps=8)
+    want = orc.cad_fit(V0, F, E, opid, 30, adam="exact")
+    assert torch.equal(out.cpu(), want), (out.cpu() - want).abs().max().item()
+    pr2 = fused.pair_from_template(pid, V0, steps=1, debug_grad=True)
+    plain = fused.StepGroupRunner(cuda, 1, pr2.ntiles, group_steps=1, use_graph=False)
+    plain.upload([pr2], [0])
+    plain.run_group()
+    assert not np.array_equal(pr2.grad_dbg.view(-1, 3).cpu().numpy(), ref)
