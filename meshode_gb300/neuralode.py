@@ -165,11 +165,12 @@ class _Backward:
              ptr(gz3), ptr(gz2), ptr(self.gu[s]), ptr(part), stream_ptr())
         return self.gu[s]
 
-    def weights(self, st, grads):
-        """The parameter gradients of the step's four evaluations, added to grads."""
+    def weights(self, st, grads, stream=None):
+        """The parameter gradients of the step's four evaluations, added to
+        grads (on `stream`, default the current one)."""
         n, M = self.n, self.M
         dW1, db1, dW2, db2, dW3, db3, dW4, db4 = grads
-        s = stream_ptr()
+        s = stream_ptr(stream)
         call("mo_mlp_partial_reduce", ptr(self.partial), 4 * self.tiles * 8, ptr(self.red), ptr(dW4), ptr(db4),
              ptr(db3), ptr(db2), ptr(db1), ptr(dW1), s)
         call("mo_mlp_wgrad", ptr(self.gz), ptr(st.array(3)), 4 * n, self.splits, ptr(self.wpart), ptr(dW3), s)
@@ -214,15 +215,30 @@ class ODEFlow(Function):
         n = ckpt.shape[1]
         grads = P.grads()
         a = a_out.contiguous().float()
-        B = _Backward(n, P.M, a.device)
-        work = None if ctx.stores is not None else _StepStore(n, P.M, a.device)
+        dev = a.device
+        main = torch.cuda.current_stream(dev)
+        # The weight gradients of step k (reads of its activations and stage
+        # gradients, adds into grads) run on a side stream while the main
+        # stream recomputes and back-propagates step k-1 into the other of
+        # two buffer sets; they fill the tail waves of those launches.  All
+        # additions into grads are on the side stream, in step order.
+        side = torch.cuda.Stream(device=dev)
+        Bs = [_Backward(n, P.M, dev), _Backward(n, P.M, dev)]
+        works = [None, None] if ctx.stores is not None else [_StepStore(n, P.M, dev), _StepStore(n, P.M, dev)]
+        done = [None, None]   # side-stream event after the last use of each buffer set
+        held = [None, None]   # stored activations kept alive until the side stream is past them
         for k in reversed(range(steps)):
+            j = k & 1
+            if done[j] is not None:
+                main.wait_event(done[j])
+            B = Bs[j]
             xk = ckpt[k]
             if ctx.stores is not None:
                 st = ctx.stores[k]
-                ctx.stores[k] = None  # freed as the backward passes it
+                ctx.stores[k] = None
+                held[j] = st  # freed once its weight gradients have run
             else:
-                st = work
+                st = works[j]
                 _rk4_step(P, xk, h, st)
             us = [xk, st.u[1], st.u[2], st.u[3]]
             dk4 = a * (h / 6)
@@ -234,8 +250,15 @@ class ODEFlow(Function):
             dx += g2
             g1 = B.stage_vjp(P, st, 0, us[0], a * (h / 6) + (h / 2) * g2)
             dx += g1
-            B.weights(st, grads)
+            ready = torch.cuda.Event()
+            ready.record(main)
+            side.wait_event(ready)
+            B.weights(st, grads, stream=side)
+            done[j] = torch.cuda.Event()
+            done[j].record(side)
             a = dx
+        main.wait_stream(side)
+        held = None
         ctx.stores = None
         ctx.P = None
         return (a, None, None) + tuple(P.unpad(grads))
