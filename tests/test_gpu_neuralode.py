@@ -8,7 +8,7 @@ toward zero, the out-of-box penalty without the N-1 slab, the 0.2 cutoff) on
 the GPU grid, and the rigidity term with the fp32 rest offsets.  It is
 itself checked against FP64 central differences (h = 1e-6).  The GPU fp32
 gradients of every parameter must lie within 1e-5 of the FP64 gradient's
-scale (max |g64|) -- the spec bar.  Widths 16 and 64 run zero-padded
+scale (max |g64|), the tolerance the configuration states.  Widths 16 and 64 run zero-padded
 in the 256-wide kernels; 256 is the configuration's own width, checked on
 a small source here and at full size (50k vertices, 128^3) against FP64
 autograd on the GPU.
