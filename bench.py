@@ -453,7 +453,7 @@ def large_config(threads):
     extrapolated from a 0.2% voxel sample) and the fused step's steady state."""
     from meshode_gb300 import fused, meshgen
     from meshode_gb300 import pyDeform as PD
-    from oracle import pydeform_oracle as orc  # checker / CPU baseline only
+    from oracle import pydeform_oracle as orc  # oracle: CPU baseline only
     dev = torch.device("cuda")
     Vs, Fs, Vt, Ft = meshgen.large_pair(seed=3)
     N = 256
@@ -526,7 +526,7 @@ def pair_config(name, Vs, Fs, Vt, Ft, N, steps, graph=None, threads=1, cpu_steps
     weight rigidity^2, DF gradient masked where d >= 0.03)."""
     from meshode_gb300 import fused, layers, metrics
     from meshode_gb300 import pyDeform as PD
-    from oracle import pydeform_oracle as orc  # CPU baseline and checker
+    from oracle import pydeform_oracle as orc  # oracle: CPU baseline and Chamfer reference
     dev = torch.device("cuda")
     Vtd, Ftd = torch.from_numpy(Vt).to(dev), torch.from_numpy(Ft).to(dev)
     PD.ReleaseTemplate(PD.InitializeDeformTemplate(Vtd, Ftd, 0, N))
@@ -686,7 +686,7 @@ def solve_linear_config():
     import time as _t
     from meshode_gb300 import meshgen
     from meshode_gb300 import pyDeform as PD
-    from oracle import pydeform_oracle as orc  # the CPU path and the checker
+    from oracle import pydeform_oracle as orc  # oracle: the CPU path
     rng = np.random.Generator(np.random.PCG64(11))
     V, F = meshgen.icosphere(6)
     V = (0.4 * V + 0.5).astype(np.float32)
@@ -1014,7 +1014,7 @@ def ours_arm(args, world, rank):
         diffs = []
         for j, i in enumerate(ids):
             Vs, Fs, Vt, Ft = meshes[i]
-            from oracle import pydeform_oracle as orc  # checker only
+            from oracle import pydeform_oracle as orc  # oracle: Chamfer reference only
             sc, tr = orc.normalize_params(Vt)
             Tn = orc.normalized_double(Vt, sc, tr)
             a = last[i].out_normalized.cpu().numpy()

@@ -1,18 +1,26 @@
 /*
  * meshode_oracle.c -- CPU restatement of MeshODE's per-iteration deformation
- * hot path.  TEST INFRASTRUCTURE ONLY: this file is the checker for the CUDA
- * library in meshode_gb300/csrc.  It is loaded by the tests, by smoke() and by
- * the CPU-baseline leg of bench.py, never by the product path.
+ * hot path.  TEST INFRASTRUCTURE ONLY: this file is the oracle the CUDA
+ * library in meshode_gb300/csrc is tested against.  It is loaded by the tests,
+ * by smoke() and by the CPU-baseline leg of bench.py, never by the product
+ * path.
  *
- * Parity status: UNPINNED against the reference.  The reference (hjwdzh/MeshODE)
- * cannot be compiled here (Eigen, Ceres, libigl and CGAL are un-vendored
- * submodules) and ships no tests or golden vectors.  Every function below is a
- * line-by-line restatement of the cited reference loop, in the same arithmetic
- * type and the same operation order, so that it reproduces the reference's
- * results bit for bit on an IEEE-754 machine without FMA contraction (the
- * reference builds with g++ -O2 for x86-64, which has no FMA by default).  The
- * file must therefore be compiled with -ffp-contract=off (aarch64 gcc contracts
- * by default).
+ * Every function below is a line-by-line restatement of the cited reference
+ * loop, in the same arithmetic type and the same operation order, so that it
+ * reproduces the reference's results bit for bit on an IEEE-754 machine
+ * without FMA contraction (the reference builds with g++ -O2 for x86-64,
+ * which has no FMA by default).  The file must therefore be compiled with
+ * -ffp-contract=off (aarch64 gcc contracts by default).
+ *
+ * Parity status: pinned.  oracle/build_ref.py compiles the reference's own
+ * source files (mesh.cc, uniformgrid.cc, the interface layers) unchanged
+ * against small stand-in headers for Eigen, ceres::Jet, torch and libigl into
+ * oracle/_ref, and tests/test_ref_pin.py checks this file against it bit for
+ * bit on the reference's demo meshes and on probes at every branch;
+ * tests/golden/gen_ref_fixtures.py keeps fixtures from it for machines
+ * without the reference.  Still unpinned: libigl's own point-mesh distance
+ * (its stand-in is the exact FP64 distance below) and the published
+ * arithmetic of Ceres and Eigen, which the stand-ins restate.
  *
  * Third-party arithmetic restated here:
  *   - ceres::Jet<float,3> (forward-mode dual numbers, version not pinned by the

@@ -1,13 +1,14 @@
 """CPU oracle with the reference's ``pyDeform`` interface (test infrastructure).
 
-This module is the checker for ``meshode_gb300.pyDeform``: it restates the
-reference's pybind11 module (src/interface/pydeform.cc:14-39) on CPU float32
-tensors, calling the C restatement in ``meshode_oracle.c`` through ctypes.
-Only tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py``
-import it.
+This module is the oracle ``meshode_gb300.pyDeform`` is tested against: it
+restates the reference's pybind11 module (src/interface/pydeform.cc:14-39) on
+CPU float32 tensors, calling the C restatement in ``meshode_oracle.c`` through
+ctypes.  Only tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import it.
 
-Parity status: UNPINNED against the reference (the reference cannot be built
-here and ships no golden vectors); see the header of meshode_oracle.c.
+Parity status: pinned against the reference's own sources compiled in
+``oracle/_ref`` (``tests/test_ref_pin.py``); see the header of
+meshode_oracle.c for what remains unpinned.
 """
 import ctypes
 import os
