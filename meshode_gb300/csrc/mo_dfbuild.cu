@@ -659,21 +659,40 @@ static void launch_df_lbvh(int packet, const float4* nodes, const float4* tris, 
 #undef MO_ARGS
 }
 
-// Brute force: each thread one voxel, triangles staged through shared memory.
+// Brute force: one warp per packet of 4 x 4 x 2 voxels with two voxels per
+// lane (the packet and the one 2 above it in z, so a warp covers 4 x 4 x 4),
+// triangles staged through shared memory in chunks and each tested against
+// both voxels of a lane at once on the packed FP32 pipe (tri_d2_2, the same
+// IEEE operations per voxel as tri_d2).  A compact packet lets the
+// warp-wide plane-distance cull skip most tests; a skipped test could not
+// have lowered any lane's best, so every voxel gets the minimum over all
+// triangles, as a test of every pair would.
 constexpr int BF_THREADS = 256, BF_CHUNK = 128;
+constexpr int BF_PX = 4, BF_PY = 4, BF_PZ = 2;
+
+__device__ __forceinline__ int64_t bf_bricks(int N) {
+    return (int64_t)((N + BF_PX - 1) / BF_PX) * ((N + BF_PY - 1) / BF_PY) * ((N + 2 * BF_PZ - 1) / (2 * BF_PZ));
+}
 
 __global__ void __launch_bounds__(BF_THREADS) k_df_brute(const float4* __restrict__ tris, int ntri, int N,
                                                          float band, float band2, float* __restrict__ grid) {
     __shared__ float4 sh[BF_CHUNK * TRI_F4];
-    const int64_t v = (int64_t)blockIdx.x * BF_THREADS + threadIdx.x;
-    const int64_t nvox = (int64_t)N * N * N;
-    const bool valid = v < nvox;
-    const int x = (int)(v % N), y = (int)((v / N) % N), z = (int)(v / ((int64_t)N * N));
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int bx = (N + BF_PX - 1) / BF_PX, by = (N + BF_PY - 1) / BF_PY;
+    const int64_t brick = (int64_t)blockIdx.x * (BF_THREADS / 32) + w;
+    // a warp past the last packet still stages triangles with its block
+    const bool live = brick < bf_bricks(N);
+    const int64_t b = live ? brick : 0;
+    const int ix = (int)(b % bx), iy = (int)((b / bx) % by), iz = (int)(b / ((int64_t)bx * by));
+    const int x = ix * BF_PX + (lane % BF_PX), y = iy * BF_PY + ((lane / BF_PX) % BF_PY);
+    const int za = iz * 2 * BF_PZ + lane / (BF_PX * BF_PY), zb = za + BF_PZ;
+    const bool va = live && x < N && y < N && za < N, vb = live && x < N && y < N && zb < N;
     const float Nf = (float)N;
-    const float px = __fdiv_rn((float)x, Nf), py = __fdiv_rn((float)y, Nf), pz = __fdiv_rn((float)z, Nf);
-    const VoxelBand vb = voxel_band(x, y, z, N, band, band2);
-    const float init = vb.bound2;
-    float best = init;
+    const float fx = __fdiv_rn((float)x, Nf), fy = __fdiv_rn((float)y, Nf);
+    const float2 px = bc2(fx), py = bc2(fy);
+    const float2 pz = make_float2(__fdiv_rn((float)za, Nf), __fdiv_rn((float)zb, Nf));
+    const VoxelBand ba = voxel_band(x, y, za, N, band, band2), bb = voxel_band(x, y, zb, N, band, band2);
+    float2 best = make_float2(ba.bound2, bb.bound2);
     for (int base = 0; base < ntri; base += BF_CHUNK) {
         const int cnt = min(BF_CHUNK, ntri - base);
         __syncthreads();
@@ -683,10 +702,13 @@ __global__ void __launch_bounds__(BF_THREADS) k_df_brute(const float4* __restric
             Tri T;
             T.r0 = sh[TRI_F4 * t]; T.r1 = sh[TRI_F4 * t + 1]; T.r2 = sh[TRI_F4 * t + 2];
             T.r3 = sh[TRI_F4 * t + 3]; T.r4 = sh[TRI_F4 * t + 4];
-            best = fminf(best, tri_d2(px, py, pz, T, valid ? best : -1.0f));
+            const float2 d = tri_d2_2(px, py, pz, T, make_float2(va ? best.x : -1.0f, vb ? best.y : -1.0f));
+            best.x = fminf(best.x, d.x);
+            best.y = fminf(best.y, d.y);
         }
     }
-    if (valid) grid[v] = best < init ? __fsqrt_rn(best) : vb.value;
+    if (va) grid[((int64_t)za * N + y) * N + x] = best.x < ba.bound2 ? __fsqrt_rn(best.x) : ba.value;
+    if (vb) grid[((int64_t)zb * N + y) * N + x] = best.y < bb.bound2 ? __fsqrt_rn(best.y) : bb.value;
 }
 
 // ---------------------------------------------------------------------------
@@ -908,7 +930,10 @@ static int df_build_impl(const float* V, int64_t nv, const int32_t* F, int64_t n
             k_check_faces<<<ceil_div(nf, 256), 256, 0, s>>>(F, nf, nv, st); ::mo::note_launch();
             k_tri_records<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, nullptr, S.tris, nullptr); ::mo::note_launch();
             const int64_t nvox = (int64_t)N * N * N;
-            k_df_brute<<<ceil_div(nvox, BF_THREADS), BF_THREADS, 0, s>>>(S.tris, (int)nf, N, band, band2, grid_out);
+            const int64_t bricks = (int64_t)((N + BF_PX - 1) / BF_PX) * ((N + BF_PY - 1) / BF_PY) *
+                                   ((N + 2 * BF_PZ - 1) / (2 * BF_PZ));
+            k_df_brute<<<ceil_div(bricks, BF_THREADS / 32), BF_THREADS, 0, s>>>(S.tris, (int)nf, N, band, band2,
+                                                                              grid_out);
             ::mo::note_launch();
             if (counts) {  // every voxel tests every triangle
                 k_add_u64<<<1, 1, 0, s>>>(counts + 1, (unsigned long long)nvox * (unsigned long long)nf);
