@@ -37,6 +37,7 @@
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #ifdef _OPENMP
 #include <omp.h>
@@ -574,22 +575,46 @@ EXPORT int orc_point_mesh_sqdist(const double* P, int64_t np, const double* V, i
 
 /* DF through the AABB tree over a list of voxels (all when vox == NULL).
  * nthreads <= 0 uses every OpenMP thread. Returns 0 on success. */
+static double wall_seconds(void) {
+    struct timespec ts;
+    timespec_get(&ts, TIME_UTC);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+/* orc_df_bvh with its two phases timed: the serial tree build (t[0]) and the
+ * voxel queries (t[1]), in seconds (for bounded CPU timings that scale only
+ * the queries to a full grid). */
+static int df_bvh_impl(const double* Vn, const int* F, int64_t nf, int N, const int64_t* vox, int64_t nvox,
+                       double* out, int nthreads, double* t);
+
 EXPORT int orc_df_bvh(const double* Vn, const int* F, int64_t nf, int N,
                       const int64_t* vox, int64_t nvox, double* out, int nthreads) {
+    return df_bvh_impl(Vn, F, nf, N, vox, nvox, out, nthreads, NULL);
+}
+
+EXPORT int orc_df_bvh_timed(const double* Vn, const int* F, int64_t nf, int N, const int64_t* vox, int64_t nvox,
+                            double* out, int nthreads, double* t2) {
+    return df_bvh_impl(Vn, F, nf, N, vox, nvox, out, nthreads, t2);
+}
+
+static int df_bvh_impl(const double* Vn, const int* F, int64_t nf, int N, const int64_t* vox, int64_t nvox,
+                       double* out, int nthreads, double* t) {
     if (nf <= 0) return -1;
-    btree t;
-    t.V = Vn; t.F = F; t.nn = 0;
-    t.order = (int*)malloc(sizeof(int) * (size_t)nf);
-    t.cen = (double*)malloc(sizeof(double) * 3 * (size_t)nf);
-    t.nodes = (bnode*)malloc(sizeof(bnode) * 2 * (size_t)nf);
-    if (!t.order || !t.cen || !t.nodes) { free(t.order); free(t.cen); free(t.nodes); return -2; }
+    const double t0 = t ? wall_seconds() : 0.0;
+    btree bt;
+    bt.V = Vn; bt.F = F; bt.nn = 0;
+    bt.order = (int*)malloc(sizeof(int) * (size_t)nf);
+    bt.cen = (double*)malloc(sizeof(double) * 3 * (size_t)nf);
+    bt.nodes = (bnode*)malloc(sizeof(bnode) * 2 * (size_t)nf);
+    if (!bt.order || !bt.cen || !bt.nodes) { free(bt.order); free(bt.cen); free(bt.nodes); return -2; }
     for (int64_t f = 0; f < nf; ++f) {
-        t.order[f] = (int)f;
+        bt.order[f] = (int)f;
         for (int c = 0; c < 3; ++c)
-            t.cen[3 * f + c] = (Vn[3 * (int64_t)F[3 * f] + c] + Vn[3 * (int64_t)F[3 * f + 1] + c] +
+            bt.cen[3 * f + c] = (Vn[3 * (int64_t)F[3 * f] + c] + Vn[3 * (int64_t)F[3 * f + 1] + c] +
                                 Vn[3 * (int64_t)F[3 * f + 2] + c]) / 3.0;
     }
-    btree_build(&t, 0, (int)nf);
+    btree_build(&bt, 0, (int)nf);
+    const double t1 = t ? wall_seconds() : 0.0;
 #ifdef _OPENMP
     int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
 #pragma omp parallel for schedule(dynamic, 64) num_threads(nt)
@@ -597,9 +622,13 @@ EXPORT int orc_df_bvh(const double* Vn, const int* F, int64_t nf, int N,
     for (int64_t q = 0; q < nvox; ++q) {
         int64_t idx = vox ? vox[q] : q;
         double p[3]; voxel_pos(idx, N, p);
-        out[q] = sqrt(btree_query(&t, p, DBL_MAX));
+        out[q] = sqrt(btree_query(&bt, p, DBL_MAX));
     }
-    free(t.order); free(t.cen); free(t.nodes);
+    if (t) {
+        t[0] = t1 - t0;
+        t[1] = wall_seconds() - t1;
+    }
+    free(bt.order); free(bt.cen); free(bt.nodes);
     return 0;
 }
 

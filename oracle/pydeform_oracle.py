@@ -50,6 +50,8 @@ def lib():
         L.orc_df_bruteforce.argtypes = [P, P, i64, ctypes.c_int, P, i64, P]
         L.orc_df_bvh.restype = ctypes.c_int
         L.orc_df_bvh.argtypes = [P, P, i64, ctypes.c_int, P, i64, P, ctypes.c_int]
+        L.orc_df_bvh_timed.restype = ctypes.c_int
+        L.orc_df_bvh_timed.argtypes = [P, P, i64, ctypes.c_int, P, i64, P, ctypes.c_int, P]
         L.orc_morton_codes.argtypes = [P, P, i64, P]
         L.orc_sort_codes.argtypes = [P, i64, P, P]
         L.orc_karras.argtypes = [P, ctypes.c_int, P, P]
@@ -118,6 +120,22 @@ def df_build(Vn64, F, N, voxels=None, method="bvh", threads=0):
         if rc != 0:
             raise RuntimeError("orc_df_bvh failed: %d" % rc)
     return out
+
+
+def df_build_timed(Vn64, F, N, voxels=None, threads=0):
+    """df_build through the AABB tree with its phases timed inside the
+    library: (values, seconds of the serial tree build, seconds of the voxel
+    queries)."""
+    Vn64 = np.ascontiguousarray(Vn64, np.float64)
+    F = _i32(F)
+    vox = None if voxels is None else np.ascontiguousarray(voxels, np.int64)
+    nvox = N ** 3 if vox is None else vox.shape[0]
+    out = np.empty(max(nvox, 1), np.float64)
+    t = np.zeros(2, np.float64)
+    rc = lib().orc_df_bvh_timed(_p(Vn64), _p(F), F.shape[0], N, _p(vox), nvox, _p(out), threads, _p(t))
+    if rc != 0:
+        raise RuntimeError("orc_df_bvh_timed failed: %d" % rc)
+    return out[:nvox], float(t[0]), float(t[1])
 
 
 def distance_float(grid, N, p):

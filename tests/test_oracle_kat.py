@@ -35,6 +35,25 @@ def test_point_triangle_regions(orc):
     assert _d2(orc, [0.0, 3.0, 4.0], a, a, a) == pytest.approx(25.0)
 
 
+def test_timed_df_build_matches_untimed(orc):
+    """The timed AABB-tree build (used for bounded CPU timings) returns the
+    untimed build's values, on the whole grid and on a z-slab sample, with
+    non-negative phase times."""
+    from meshode_gb300 import meshgen
+    V, F = meshgen.icosphere(2)
+    Vn = 0.5 + 0.4 * np.asarray(V, np.float64)
+    N = 12
+    whole = orc.df_build(Vn, F, N)
+    vals, t_tree, t_query = orc.df_build_timed(Vn, F, N)
+    assert np.array_equal(vals, whole) and t_tree >= 0.0 and t_query >= 0.0
+    zs = np.arange(1, N, 4)
+    vox = (zs[:, None] * N * N + np.arange(N * N)[None, :]).ravel().astype(np.int64)
+    part, _, _ = orc.df_build_timed(Vn, F, N, voxels=vox)
+    assert np.array_equal(part, whole[vox])
+    empty, _, _ = orc.df_build_timed(Vn, F, N, voxels=np.zeros(0, np.int64))
+    assert empty.shape == (0,)
+
+
 def test_trilinear_reproduces_linear_field(orc):
     N = 16
     z, y, x = np.meshgrid(np.arange(N), np.arange(N), np.arange(N), indexing="ij")
