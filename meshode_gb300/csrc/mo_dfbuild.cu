@@ -670,7 +670,7 @@ static void launch_df_lbvh(int packet, const float4* nodes, const float4* tris, 
 constexpr int BF_THREADS = 256, BF_CHUNK = 128;
 constexpr int BF_PX = 4, BF_PY = 4, BF_PZ = 2;
 
-__device__ __forceinline__ int64_t bf_bricks(int N) {
+__host__ __device__ __forceinline__ int64_t bf_bricks(int N) {
     return (int64_t)((N + BF_PX - 1) / BF_PX) * ((N + BF_PY - 1) / BF_PY) * ((N + 2 * BF_PZ - 1) / (2 * BF_PZ));
 }
 
@@ -930,10 +930,8 @@ static int df_build_impl(const float* V, int64_t nv, const int32_t* F, int64_t n
             k_check_faces<<<ceil_div(nf, 256), 256, 0, s>>>(F, nf, nv, st); ::mo::note_launch();
             k_tri_records<<<ceil_div(nf, 256), 256, 0, s>>>(S.Vn, F, nf, nv, nullptr, S.tris, nullptr); ::mo::note_launch();
             const int64_t nvox = (int64_t)N * N * N;
-            const int64_t bricks = (int64_t)((N + BF_PX - 1) / BF_PX) * ((N + BF_PY - 1) / BF_PY) *
-                                   ((N + 2 * BF_PZ - 1) / (2 * BF_PZ));
-            k_df_brute<<<ceil_div(bricks, BF_THREADS / 32), BF_THREADS, 0, s>>>(S.tris, (int)nf, N, band, band2,
-                                                                              grid_out);
+            k_df_brute<<<ceil_div(bf_bricks(N), BF_THREADS / 32), BF_THREADS, 0, s>>>(S.tris, (int)nf, N, band,
+                                                                                   band2, grid_out);
             ::mo::note_launch();
             if (counts) {  // every voxel tests every triangle
                 k_add_u64<<<1, 1, 0, s>>>(counts + 1, (unsigned long long)nvox * (unsigned long long)nf);
