@@ -254,6 +254,13 @@ int mo_edge_forward_w(const float* V, int64_t nv, const int32_t* idx, int64_t n_
                       const float* off, const float* w, float* loss_out, void* stream);
 int mo_edge_backward_w(const float* V, int64_t nv, const void* csr, int64_t nh, const float* off,
                        const float* w, float* grad_out, void* stream);
+/* One evaluation of the edge term: loss_out [H,3] as mo_edge_forward_w
+ * (NULL: not computed) and grad_out [nv,3] as mo_edge_backward_w, for the
+ * half-edges of idx (kind) whose CSR (mo_edge_csr_build over the same idx)
+ * is csr; w NULL: weight 1 (RigidEdgeLoss / GraphEdgeLoss), else the
+ * CadEdgeLoss weights.  Same results as the two calls. */
+int mo_edge_fwd_bwd(const float* V, int64_t nv, const int32_t* idx, int64_t n_items, int kind, const void* csr,
+                    const float* off, const float* w, float* loss_out, float* grad_out, void* stream);
 
 /* Sliced-ELL (32-vertex slices, column-major records) view of the CSR for
  * the fused step: one int32 record per incident half-edge, other | role<<31

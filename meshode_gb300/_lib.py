@@ -115,6 +115,7 @@ _SIGS = {
     "mo_edge_cad_weights": (_I, [_P, _I64, _P, _P]),
     "mo_edge_forward_w": (_I, [_P, _I64, _P, _I64, _I, _P, _P, _P, _P]),
     "mo_edge_backward_w": (_I, [_P, _I64, _P, _I64, _P, _P, _P, _P]),
+    "mo_edge_fwd_bwd": (_I, [_P, _I64, _P, _I64, _I, _P, _P, _P, _P, _P, _P]),
     "mo_sell_plan": (_I, [_P, _I64, _I64, _P, _P]),
     "mo_sell_fill": (_I, [_P, _I64, _I64, _P, _P, _P]),
     "mo_sell_fill_w": (_I, [_P, _I64, _I64, _P, _P, _P, _P]),

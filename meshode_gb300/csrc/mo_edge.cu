@@ -473,6 +473,20 @@ extern "C" int mo_edge_backward_w(const float* V, int64_t nv, const void* csr, i
     return MO_OK;
 }
 
+extern "C" int mo_edge_fwd_bwd(const float* V, int64_t nv, const int32_t* idx, int64_t n_items, int kind,
+                               const void* csr, const float* off, const float* w, float* loss_out,
+                               float* grad_out, void* stream) {
+    int64_t nh;
+    int rc = check_edges(V, nv, idx, n_items, kind, &nh);
+    if (rc) return rc;
+    MO_CHECK_ARG(grad_out && (nv == 0 || csr), "null gradient or CSR pointer");
+    if (loss_out) {
+        rc = mo_edge_forward_w(V, nv, idx, n_items, kind, off, w, loss_out, stream);
+        if (rc) return rc;
+    }
+    return mo_edge_backward_w(V, nv, csr, nh, off, w, grad_out, stream);
+}
+
 extern "C" int mo_sell_plan(const void* csr, int64_t nv, int64_t nh, int32_t* slice_ptr, void* stream) {
     MO_CHECK_ARG(nv >= 0 && nh >= 0, "negative size");
     MO_CHECK_ARG(csr && slice_ptr, "null pointer");

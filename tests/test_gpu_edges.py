@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 import torch
 
+from meshode_gb300 import _lib as L
 from meshode_gb300 import meshgen
 from meshode_gb300 import pyDeform as PD
 
@@ -50,6 +51,15 @@ def test_rigid_edges_bitexact(cuda, orc, level):
         assert ok, n
         ok, n = _same(b, orc.edge_backward(V1, F, 0, off))
         assert ok, n
+    # the combined entry point (no weights) gives the two calls' results
+    st = PD.GetParams(pid).edge
+    Vx = torch.from_numpy(V1).to(cuda)
+    loss = torch.empty(st.nh, 3, dtype=torch.float32, device=cuda)
+    grad = torch.empty(Vx.shape[0], 3, dtype=torch.float32, device=cuda)
+    L.call("mo_edge_fwd_bwd", L.ptr(Vx), Vx.shape[0], L.ptr(st.idx), F.shape[0], L.MO_EDGES_FACES, L.ptr(st.csr),
+           L.ptr(st.offsets), None, L.ptr(loss), L.ptr(grad), L.stream_ptr())
+    assert torch.equal(loss, PD.RigidEdgeLoss_forward(Vx, Ft.to(cuda), pid))
+    assert torch.equal(grad, PD.RigidEdgeLoss_backward(Vx, Ft.to(cuda), pid))
 
 
 def test_graph_edges_degenerate_and_duplicates(cuda, orc):
@@ -144,3 +154,12 @@ def test_cad_edges_bitexact(cuda, orc, level):
         assert ok, n
     with pytest.raises(RuntimeError):
         PD.RigidEdgeLoss_forward(torch.from_numpy(V1), Ft, pid)  # the template holds CAD edges now
+    # the combined entry point gives the two calls' results
+    Vx = torch.from_numpy(V1).to(cuda)
+    _, st_, Vd, lst, csr = PD._cad_state(pid, Vx, Ft.to(cuda), Et.to(cuda))
+    loss = torch.empty(st_.nh, 3, dtype=torch.float32, device=cuda)
+    grad = torch.empty(Vd.shape[0], 3, dtype=torch.float32, device=cuda)
+    L.call("mo_edge_fwd_bwd", L.ptr(Vd), Vd.shape[0], L.ptr(lst), st_.nh, L.MO_EDGES_LIST, L.ptr(csr),
+           L.ptr(st_.offsets), L.ptr(st_.weights), L.ptr(loss), L.ptr(grad), L.stream_ptr())
+    assert torch.equal(loss, PD.CadEdgeLoss_forward(Vx, Ft.to(cuda), Et.to(cuda), pid))
+    assert torch.equal(grad, PD.CadEdgeLoss_backward(Vx, Ft.to(cuda), Et.to(cuda), pid))
