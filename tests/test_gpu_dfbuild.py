@@ -29,8 +29,10 @@ def _diag(Vn64):
 
 
 @pytest.mark.parametrize("method", [L.MO_DF_BRUTE, L.MO_DF_LBVH])
-@pytest.mark.parametrize("level,N", [(0, 8), (2, 24), (3, 32)])
+@pytest.mark.parametrize("level,N", [(0, 8), (2, 24), (3, 32), (0, 7), (1, 13)])
 def test_df_vs_fp64(cuda, orc, method, level, N):
+    """Both methods against the FP64 oracle, including grids whose size is
+    not a multiple of the voxel packets (partial packets at the far faces)."""
     V, F = _target(level, seed=level + 1)
     pid = PD.InitializeDeformTemplate(torch.from_numpy(V), torch.from_numpy(F), 0, N, df_method=method)
     g = PD.GetDistanceField(pid).cpu().numpy().reshape(-1).astype(np.float64)
@@ -41,6 +43,10 @@ def test_df_vs_fp64(cuda, orc, method, level, N):
     ref = orc.df_build(Vn, F, N, method="brute")
     err = np.abs(g - ref).max()
     assert err <= TOL_REL_DIAG * _diag(Vn), (err, _diag(Vn))
+    other = L.MO_DF_LBVH if method == L.MO_DF_BRUTE else L.MO_DF_BRUTE
+    pid2 = PD.InitializeDeformTemplate(torch.from_numpy(V), torch.from_numpy(F), 0, N, df_method=other)
+    assert torch.equal(PD.GetDistanceField(pid), PD.GetDistanceField(pid2))  # the two methods, bit for bit
+    PD.ReleaseTemplate(pid2)
 
 
 def test_df_lbvh_large_subsampled(cuda, orc):
