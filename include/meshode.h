@@ -96,8 +96,8 @@ int mo_lbvh_build(const float* V, int64_t nv, const int32_t* F, int64_t nf, cons
  * fixed device array of MO_DF_NOALLOC_SCRATCH_BYTES that every GPU loading
  * this library holds until the process exits; targets whose scratch need
  * (mo_df_build_scratch_bytes with mo_df_method_for's method) exceeds it are
- * rejected with MO_ERR_SCRATCH.  The LBVH build needs about 427 bytes per
- * triangle plus 12 per vertex, so the array holds targets of up to 19,000
+ * rejected with MO_ERR_SCRATCH.  The LBVH build needs about 405 bytes per
+ * triangle plus 12 per vertex, so the array holds targets of up to 20,000
  * triangles with up to 10,000 vertices (a closed mesh has about half as
  * many vertices as triangles).  The caller still passes the inputs and the
  * output grid.  The first call on a device, made with that device current,
@@ -171,9 +171,10 @@ int mo_df_build_count(const float* V, int64_t nv, const int32_t* F, int64_t nf, 
 float mo_df_loss_band(int N);
 /* The target's traversal tree alone, for on-demand fills (mo_df_lazy_fill):
  * the steps of the LBVH build of mo_df_build_ex without the grid pass.
- * tree_out (mo_df_tree_bytes(nf) bytes, 16-byte aligned) gets the sorted
- * triangle records (80 B each), then the internal nodes' traversal records
- * (144 B each).  scratch:
+ * tree_out (mo_df_tree_bytes(nf) bytes, 16-byte aligned; 128-byte aligned
+ * puts every node record in one cache line) gets the sorted triangle
+ * records (80 B each), padded to a multiple of 128 B, then the internal
+ * nodes' traversal records (128 B each); nf <= 2^27.  scratch:
  * mo_df_tree_scratch_bytes; status_out (device int32) gets bit 1 for a face
  * index out of range.  Nothing is synchronised. */
 size_t mo_df_tree_bytes(int64_t nf);

@@ -104,19 +104,39 @@ __device__ __forceinline__ float dotf3(float3 a, float x, float y, float z) {
     return fmaf(a.z, z, fmaf(a.y, y, __fmul_rn(a.x, x)));
 }
 
-// Traversal record of an internal node: NODE_F4 float4 holding both
+// Traversal record of an internal node: NODE_F4 float4 (128 bytes, one
+// cache line when the record array is 128-byte aligned) holding both
 // children's oriented boxes interleaved, each float2 (left, right), so that
 // one packed FP32 pass (FFMA2 / FADD2) bounds both children:
 //   w0 = (-o.x, -o.y)  w1 = (-o.z, -e.x)  w2 = (a1.x, a1.y)  w3 = (a1.z, -e.y)
 //   w4 = (a2.x, a2.y)  w5 = (a2.z, -e.z)  w6 = (a3.x, a3.y)  w7 = (a3.z, id)
-//   w8 = (left count, right count, 0, 0) as ints
 // where each named component is a (left, right) pair: w0 = (-oL.x, -oR.x,
 // -oL.y, -oR.y) and so on.  o: a box's origin corner, a1..a3 its axes
 // (a3 = obb_a3(a1, a2), stored so the walk does not recompute it), e its
-// extents (origin and extents stored negated: the walk adds them); id >= 0
-// an internal node, ~first for a bucket of `count` (1..DF_BUCKET) sorted
-// triangles (count 0: internal).
-constexpr int NODE_F4 = 9;
+// extents (origin and extents stored negated: the walk adds them); id (an
+// int) >= 0 an internal node, or ~(first | count << BUCKET_SHIFT) for a
+// bucket of `count` (1..DF_BUCKET) sorted triangles from `first`
+// (first < 2^BUCKET_SHIFT).
+constexpr int NODE_F4 = 8;
+constexpr int BUCKET_SHIFT = 27;
+constexpr int64_t MAX_TREE_TRIANGLES = (int64_t)1 << BUCKET_SHIFT;
+
+__host__ __device__ __forceinline__ int pack_child(int id, int count) {
+    return count > 0 ? ~((~id) | (count << BUCKET_SHIFT)) : id;
+}
+// bucket size of a packed child (0: internal node)
+__device__ __forceinline__ int child_count(int packed) { return packed < 0 ? ((~packed) >> BUCKET_SHIFT) : 0; }
+// the child as the walk indexes it: the node, or ~first of a bucket
+__device__ __forceinline__ int child_id(int packed) {
+    return packed < 0 ? ~((~packed) & ((1 << BUCKET_SHIFT) - 1)) : packed;
+}
+
+// Offset (float4) of the node records behind the triangle records in a
+// traversal tree buffer (mo_df_tree_build): the triangles rounded up to 128
+// bytes, so that a 128-byte aligned buffer aligns every node record.
+__host__ __device__ __forceinline__ int64_t tree_nodes_offset_f4(int64_t ntri) {
+    return (TRI_F4 * ntri + 7) & ~(int64_t)7;
+}
 
 __device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
 __device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
@@ -375,9 +395,9 @@ __device__ __forceinline__ float df_voxel_value(const float4* __restrict__ nodes
             const float4* nd = nodes + NODE_F4 * (int64_t)node;
             const float4 w0 = __ldg(nd), w1 = __ldg(nd + 1), w2 = __ldg(nd + 2), w3 = __ldg(nd + 3);
             const float4 w4 = __ldg(nd + 4), w5 = __ldg(nd + 5), w6 = __ldg(nd + 6), w7 = __ldg(nd + 7);
-            const int2 cnt = __ldg(reinterpret_cast<const int2*>(nd + 8));
-            const int L = __float_as_int(w7.z), R = __float_as_int(w7.w);
-            const int cl = cnt.x, cr = cnt.y;  // bucket sizes (0: internal)
+            const int Lp = __float_as_int(w7.z), Rp = __float_as_int(w7.w);
+            const int L = child_id(Lp), R = child_id(Rp);
+            const int cl = child_count(Lp), cr = child_count(Rp);  // bucket sizes (0: internal)
             const float2 dlr = obb_pair_d2(P2x, P2y, P2z, w0, w1, w2, w3, w4, w5, w6, w7);
             const float dl = dlr.x, dr = dlr.y;
             bool wl = __any_sync(FULL, dl < lim);
@@ -487,9 +507,9 @@ __device__ __forceinline__ float2 df_voxel_value2(const float4* __restrict__ nod
             const float4* nd = nodes + NODE_F4 * (int64_t)node;
             const float4 w0 = __ldg(nd), w1 = __ldg(nd + 1), w2 = __ldg(nd + 2), w3 = __ldg(nd + 3);
             const float4 w4 = __ldg(nd + 4), w5 = __ldg(nd + 5), w6 = __ldg(nd + 6), w7 = __ldg(nd + 7);
-            const int2 cnt = __ldg(reinterpret_cast<const int2*>(nd + 8));
-            const int L = __float_as_int(w7.z), R = __float_as_int(w7.w);
-            const int cl = cnt.x, cr = cnt.y;
+            const int Lp = __float_as_int(w7.z), Rp = __float_as_int(w7.w);
+            const int L = child_id(Lp), R = child_id(Rp);
+            const int cl = child_count(Lp), cr = child_count(Rp);
             const float2 dl = obb_d2_2<0>(px, py, pz, w0, w1, w2, w3, w4, w5, w6, w7);
             const float2 dr = obb_d2_2<1>(px, py, pz, w0, w1, w2, w3, w4, w5, w6, w7);
             bool wl = __any_sync(FULL, dl.x < lim.x || dl.y < lim.y);

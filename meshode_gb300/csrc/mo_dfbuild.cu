@@ -565,8 +565,8 @@ __global__ void k_obb_nodes(const float4* __restrict__ nodes, const int2* __rest
     t[4] = make_float4(L.a2.x, R.a2.x, L.a2.y, R.a2.y);
     t[5] = make_float4(L.a2.z, R.a2.z, -L.e.z, -R.e.z);
     t[6] = make_float4(a3s[0].x, a3s[1].x, a3s[0].y, a3s[1].y);
-    t[7] = make_float4(a3s[0].z, a3s[1].z, __int_as_float(ids[0]), __int_as_float(ids[1]));
-    t[8] = make_float4(__int_as_float(cnts[0]), __int_as_float(cnts[1]), 0.f, 0.f);
+    t[7] = make_float4(a3s[0].z, a3s[1].z, __int_as_float(pack_child(ids[0], cnts[0])),
+                       __int_as_float(pack_child(ids[1], cnts[1])));
 }
 
 // The full grid: one warp per packet of PX x PY x PZ voxels.
@@ -805,7 +805,7 @@ using namespace mo;
 
 extern "C" size_t mo_df_tree_bytes(int64_t nf) {
     if (nf <= 0) return 0;
-    return sizeof(float4) * ((size_t)TRI_F4 * nf + NODE_F4 * (size_t)(nf > 1 ? nf - 1 : 1));
+    return sizeof(float4) * ((size_t)tree_nodes_offset_f4(nf) + NODE_F4 * (size_t)(nf > 1 ? nf - 1 : 1));
 }
 
 extern "C" size_t mo_df_tree_scratch_bytes(int64_t nv, int64_t nf) {
@@ -818,7 +818,7 @@ extern "C" int mo_df_tree_build(const float* V, int64_t nv, const int32_t* F, in
                                 void* stream) {
     MO_CHECK_ARG(nv > 0 && nf > 0, "target mesh must have vertices and faces (nv=%lld nf=%lld)", (long long)nv,
                  (long long)nf);
-    MO_CHECK_ARG(nf < ((int64_t)1 << 30) && nv < ((int64_t)1 << 31), "target mesh too large");
+    MO_CHECK_ARG(nf <= MAX_TREE_TRIANGLES && nv < ((int64_t)1 << 31), "target mesh too large for the tree");
     MO_CHECK_ARG(V && F && params4 && scratch && tree_out && status_out, "null pointer");
     MO_CHECK_ARG((reinterpret_cast<uintptr_t>(tree_out) & 15) == 0, "tree_out must be 16-byte aligned");
     const size_t need = plan_scratch(nullptr, nv, nf, MO_DF_LBVH).bytes;
@@ -831,7 +831,7 @@ extern "C" int mo_df_tree_build(const float* V, int64_t nv, const int32_t* F, in
     float4* out = reinterpret_cast<float4*>(tree_out);
     // the records are written straight into the output
     S.tris = out;
-    S.tnodes = out + (size_t)TRI_F4 * nf;
+    S.tnodes = out + tree_nodes_offset_f4(nf);
     k_normalize_copy<<<ceil_div(3 * nv, 256), 256, 0, s>>>(V, nv, params4, S.Vn); ::mo::note_launch();
     cudaError_t e = issue_tree(S, F, nv, nf, reinterpret_cast<int*>(status_out), s);
     if (e != cudaSuccess) return cuda_status(e, "mo_df_tree_build");
@@ -903,6 +903,8 @@ static int df_build_impl(const float* V, int64_t nv, const int32_t* F, int64_t n
     MO_CHECK_ARG(V && F && params4 && grid_out, "null pointer");
     MO_CHECK_ARG(method == MO_DF_AUTO || method == MO_DF_BRUTE || method == MO_DF_LBVH, "unknown method %d", method);
     if (method == MO_DF_AUTO) method = mo_df_method_for(nf, N);
+    MO_CHECK_ARG(method != MO_DF_LBVH || nf <= MAX_TREE_TRIANGLES, "target mesh too large for the LBVH (%lld > %lld)",
+                 (long long)nf, (long long)MAX_TREE_TRIANGLES);
     cudaStream_t s = as_stream(stream);
     const size_t need = plan_scratch(nullptr, nv, nf, method).bytes;
     void* owned = nullptr;

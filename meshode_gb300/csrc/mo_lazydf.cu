@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) k_lazy_packets(const MoPair* 
         const float band = P.df_band;
         const float band2 = band > 0.f ? band * band : FLT_MAX;
         const float4* tris = reinterpret_cast<const float4*>(P.df_tree);
-        const float4* nodes = tris + (int64_t)TRI_F4 * P.df_ntri;
+        const float4* nodes = tris + tree_nodes_offset_f4(P.df_ntri);
         const float v = df_voxel_value(nodes, tris, P.df_ntri, N, band, band2, x, y, z, valid, stack[w],
                                        P.df_status);
         if (valid) P.df_lin[((int64_t)z * N + y) * N + x] = v;

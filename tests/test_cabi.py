@@ -127,7 +127,7 @@ def test_distance_field_entry_points_check_arguments_without_gpu():
     B.build()
     lib = L.lib()
     assert lib.mo_df_tree_bytes(0) == 0
-    assert lib.mo_df_tree_bytes(3) == 16 * (5 * 3 + 9 * 2)
+    assert lib.mo_df_tree_bytes(3) == 16 * (16 + 8 * 2)  # 15 triangle float4 padded to 16, two 128 B nodes
     assert lib.mo_df_tree_scratch_bytes(-1, 3) == 0
     assert lib.mo_df_tree_build(None, 10, None, 4, None, None, 0, None, None, None) == L.MO_ERR_INVALID
     assert b"null" in lib.mo_last_error()
@@ -144,17 +144,17 @@ def test_distance_field_entry_points_check_arguments_without_gpu():
 
 def test_noalloc_capacity_matches_documented_figure():
     """The header documents that mo_df_build_noalloc's fixed array holds
-    targets of up to 19,000 triangles with up to 10,000 vertices; the
+    targets of up to 20,000 triangles with up to 10,000 vertices; the
     library's own scratch planner must agree, so the figure cannot drift."""
     B.build()
     lib = L.lib()
     cap = lib.mo_df_noalloc_scratch_capacity()
     src = open(HEADER).read()
-    assert "19,000" in src and "10,000 vertices" in src
-    assert lib.mo_df_method_for(19_000, 64) == L.MO_DF_LBVH
+    assert "20,000" in src and "10,000 vertices" in src
+    assert lib.mo_df_method_for(20_000, 64) == L.MO_DF_LBVH
     for N in (32, 64, 128, 256):
-        m = lib.mo_df_method_for(19_000, N)
-        assert lib.mo_df_build_scratch_bytes(10_000, 19_000, N, m) <= cap
-        # about 5% more triangles no longer fit
         m = lib.mo_df_method_for(20_000, N)
-        assert lib.mo_df_build_scratch_bytes(10_000, 20_000, N, m) > cap
+        assert lib.mo_df_build_scratch_bytes(10_000, 20_000, N, m) <= cap
+        # about 5% more triangles no longer fit
+        m = lib.mo_df_method_for(21_000, N)
+        assert lib.mo_df_build_scratch_bytes(10_000, 21_000, N, m) > cap

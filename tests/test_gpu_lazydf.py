@@ -122,7 +122,7 @@ def test_lazy_arguments_are_checked(cuda):
     lib = L.lib()
     assert lib.mo_df_lazy_bytes(1) == 0 and lib.mo_df_lazy_bytes(L.MO_DF_LAZY_MAX_N + 1) == 0
     assert lib.mo_df_lazy_bytes(64) == 4 * ((63 ** 3 + 31) // 32 + (16 * 16 * 32 + 31) // 32)
-    assert lib.mo_df_tree_bytes(0) == 0 and lib.mo_df_tree_bytes(10) == 16 * (5 * 10 + 9 * 9)
+    assert lib.mo_df_tree_bytes(0) == 0 and lib.mo_df_tree_bytes(10) == 16 * (56 + 8 * 9)  # 50 triangle float4 padded to 56
     assert lib.mo_df_lazy_fill(None, None, None, None, 0, None, None) == L.MO_ERR_INVALID
     assert lib.mo_df_tree_build(None, 0, None, 0, None, None, 0, None, None, None) == L.MO_ERR_INVALID
 
