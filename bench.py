@@ -246,6 +246,7 @@ def cpu_request_model(specs, meshes, i, threads, loop_steps=50, voxel_stride=1):
     t0 = time.perf_counter()
     orc.rigid_fit(V, Ft_, pid, loop_steps)
     t_loop = (time.perf_counter() - t0) * specs[i]["steps"] / loop_steps
+    orc.ReleaseTemplate(pid)
     return t_df + t_loop, t_df, t_loop
 
 
@@ -266,6 +267,7 @@ def run_cpu_port(specs, meshes, ids, threads):
         orc.StoreRigidityInformation(V, Ft_, pid)
         out, _ = orc.rigid_fit(V, Ft_, pid, specs[i]["steps"])
         outs.append(out)
+        orc.ReleaseTemplate(pid)
     return time.perf_counter() - t0, outs
 
 

@@ -339,6 +339,13 @@ def InitializeDeformTemplate(V, F, symmetry, N, df_method="bvh", grid=None):
     return len(_params) - 1
 
 
+def ReleaseTemplate(pid):
+    """Drop a template's state (the handle stays unused).  The reference
+    never frees its templates (deform_params.cc:7-14); this is for long
+    measuring loops that create many."""
+    _params[pid] = None
+
+
 def NormalizeByTemplate(V, pid):
     p = _params[pid]
     a = V.detach().numpy() if isinstance(V, torch.Tensor) else V
