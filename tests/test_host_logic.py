@@ -133,3 +133,35 @@ def test_cpu_baseline_strata():
     cost = {i: [float(keys.index(k))] for k in keys for i in ids if i in strata[k]}
     want = sum(len(strata[k]) / 512 * keys.index(k) for k in keys)
     assert abs(bench.stream_mean_seconds(specs, cost) - want) < 1e-12
+
+
+def test_reference_arm_covers_every_stratum_each_step(monkeypatch, capsys):
+    """bench.py --impl reference: every timed step is one pass over all 12
+    sampled requests (so a short run is not biased toward the first strata),
+    and the reported value is 1 / the stream-weighted mean of their costs."""
+    import argparse
+    import json
+    import bench
+    calls = []
+
+    def fake_model(specs, meshes, i, threads, loop_steps=50, voxel_stride=1):
+        calls.append((i, voxel_stride))
+        return 1.0 + (i % 7), 0.0, 0.0
+
+    monkeypatch.setattr(bench, "cpu_request_model", fake_model)
+    monkeypatch.setattr(bench, "run_cpu_port", lambda *a, **k: (0.0, []))
+    monkeypatch.setattr(bench, "make_stream", lambda args, seed: (_bench_specs(), [None] * 512))
+    args = argparse.Namespace(requests=512, req_steps=500, warmup=1, steps=2, gpus=1)
+    bench.reference_arm(args, 1, 0)
+    out = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    ids = bench.cpu_sample_ids(_bench_specs())
+    assert [c[0] for c in calls] == ids + ids
+    assert all(c[1] == bench.REF_VOXEL_STRIDE for c in calls)
+    want = 1.0 / bench.stream_mean_seconds(_bench_specs(), {i: [1.0 + (i % 7)] * 2 for i in ids})
+    assert abs(out["value"] - want) < 1e-12 and out["impl"] == "reference"
+    assert out["cpu_baseline"]["kind"] == "port" and out["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def _bench_specs():
+    from meshode_gb300 import meshgen
+    return meshgen.serving_requests(n=512, seed=5, steps=500)
