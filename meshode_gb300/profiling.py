@@ -1,9 +1,10 @@
 """Small, fixed workloads for profiling single kernels with ncu.
 
-    python -m meshode_gb300.profiling step --pairs 64 --groups 1
+    python -m meshode_gb300.profiling step --pairs 64 --groups 1 [--engine python]
         the first `pairs` requests of the serving stream prepared and stepped
-        together: `groups` x 25 launches of k_fused_step with every pair
-        active (plus one warm-up group);
+        together by the native pool (or the Python engine): `groups` x 25
+        launches of k_fused_step with every pair active (plus one warm-up
+        group);
     python -m meshode_gb300.profiling df --request 1 --repeat 2 [--band] [--packet 4x2x4]
         the distance-field build of one request of the stream, `repeat` times
         (--band: with the loss-preserving band the serving builds use).
@@ -18,7 +19,7 @@ import torch
 
 from . import _lib as L
 from . import build as B
-from . import autotune, meshgen, serving
+from . import autotune, meshgen, pool, serving
 
 
 def _stream(n, seed=5):
@@ -32,11 +33,15 @@ def step(args):
     reqs = serving.requests_from_meshes(meshes, specs, device=dev)
     for r in reqs:
         r.steps = 100000
-    eng = serving.ServingEngine(group_steps=25, results_to_host=False)
-    jobs = eng.prepare(reqs)
-    t, nbytes, nv = eng.steady_state(jobs, groups=args.groups)
+    if args.engine == "native":
+        eng = pool.NativePool(group_steps=25, results_to_host=False, max_pairs=max(len(reqs), 1))
+        t, nbytes, nv = eng.steady_state(reqs, groups=args.groups)
+        eng.close()
+    else:
+        eng = serving.ServingEngine(group_steps=25, results_to_host=False)
+        t, nbytes, nv = eng.steady_state(eng.prepare(reqs), groups=args.groups)
     print("k_fused_step: %d pairs, %d vertices, %.4f ms/launch, %.1f GB/s algorithmic (104V+44H)"
-          % (len(jobs), nv, t * 1e3, nbytes / t / 1e9))
+          % (len(reqs), nv, t * 1e3, nbytes / t / 1e9))
 
 
 def df(args):
@@ -81,6 +86,8 @@ def main(argv=None):
     a = sub.add_parser("step")
     a.add_argument("--pairs", type=int, default=64)
     a.add_argument("--groups", type=int, default=1)
+    a.add_argument("--engine", default="native", choices=["native", "python"],
+                   help="the native pool (mo_pool_*) or the Python engine over the same kernels")
     b = sub.add_parser("df")
     b.add_argument("--request", type=int, default=1)
     b.add_argument("--repeat", type=int, default=2)
