@@ -114,22 +114,17 @@ __device__ __forceinline__ float dotf3(float3 a, float x, float y, float z) {
 // -oL.y, -oR.y) and so on.  o: a box's origin corner, a1..a3 its axes
 // (a3 = obb_a3(a1, a2), stored so the walk does not recompute it), e its
 // extents (origin and extents stored negated: the walk adds them); id (an
-// int) >= 0 an internal node, or ~(first | count << BUCKET_SHIFT) for a
-// bucket of `count` (1..DF_BUCKET) sorted triangles from `first`
-// (first < 2^BUCKET_SHIFT).
+// int) = index << 3 | count: an internal node (count 0) and its index, or a
+// bucket of `count` (1..DF_BUCKET) sorted triangles from triangle `index`.
 constexpr int NODE_F4 = 8;
-constexpr int BUCKET_SHIFT = 27;
-constexpr int64_t MAX_TREE_TRIANGLES = (int64_t)1 << BUCKET_SHIFT;
+constexpr int64_t MAX_TREE_TRIANGLES = (int64_t)1 << 27;  // index << 3 stays an int
 
-__host__ __device__ __forceinline__ int pack_child(int id, int count) {
-    return count > 0 ? ~((~id) | (count << BUCKET_SHIFT)) : id;
-}
+// node: the child's node index (count 0), or the bucket's first triangle
+__host__ __device__ __forceinline__ int pack_child(int index, int count) { return (index << 3) | count; }
 // bucket size of a packed child (0: internal node)
-__device__ __forceinline__ int child_count(int packed) { return packed < 0 ? ((~packed) >> BUCKET_SHIFT) : 0; }
-// the child as the walk indexes it: the node, or ~first of a bucket
-__device__ __forceinline__ int child_id(int packed) {
-    return packed < 0 ? ~((~packed) & ((1 << BUCKET_SHIFT) - 1)) : packed;
-}
+__device__ __forceinline__ int child_count(int packed) { return packed & 7; }
+// the child's node index, or the first triangle of its bucket
+__device__ __forceinline__ int child_index(int packed) { return packed >> 3; }
 
 // Offset (float4) of the node records behind the triangle records in a
 // traversal tree buffer (mo_df_tree_build): the triangles rounded up to 128
@@ -396,7 +391,7 @@ __device__ __forceinline__ float df_voxel_value(const float4* __restrict__ nodes
             const float4 w0 = __ldg(nd), w1 = __ldg(nd + 1), w2 = __ldg(nd + 2), w3 = __ldg(nd + 3);
             const float4 w4 = __ldg(nd + 4), w5 = __ldg(nd + 5), w6 = __ldg(nd + 6), w7 = __ldg(nd + 7);
             const int Lp = __float_as_int(w7.z), Rp = __float_as_int(w7.w);
-            const int L = child_id(Lp), R = child_id(Rp);
+            const int L = child_index(Lp), R = child_index(Rp);
             const int cl = child_count(Lp), cr = child_count(Rp);  // bucket sizes (0: internal)
             const float2 dlr = obb_pair_d2(P2x, P2y, P2z, w0, w1, w2, w3, w4, w5, w6, w7);
             const float dl = dlr.x, dr = dlr.y;
@@ -408,10 +403,10 @@ __device__ __forceinline__ float df_voxel_value(const float4* __restrict__ nodes
             // two triangles per test where both are non-degenerate
 #pragma unroll 1
             for (int k = 0; PAIR_TRIS && k < nl + nr; k += 2) {
-                const int ta = k < nl ? ~L + k : ~R + (k - nl);
+                const int ta = k < nl ? L + k : R + (k - nl);
                 const Tri A = load_tri(tris, ta);
                 if (k + 1 < nl + nr) {
-                    const int tb = k + 1 < nl ? ~L + k + 1 : ~R + (k + 1 - nl);
+                    const int tb = k + 1 < nl ? L + k + 1 : R + (k + 1 - nl);
                     const Tri B = load_tri(tris, tb);
                     if (A.r3.w != 0.f && B.r3.w != 0.f) {  // warp-uniform
                         const float2 t = tri_d2_t2(px, py, pz, A, B, best);
@@ -430,7 +425,7 @@ __device__ __forceinline__ float df_voxel_value(const float4* __restrict__ nodes
             }
 #pragma unroll 1
             for (int k = 0; !PAIR_TRIS && k < nl + nr; ++k) {
-                const int tri = k < nl ? ~L + k : ~R + (k - nl);
+                const int tri = k < nl ? L + k : R + (k - nl);
                 const float t = tri_d2(px, py, pz, load_tri(tris, tri), best);
                 if (valid && t < best) { best = t; lim = slack_bound(best); }
             }
@@ -508,7 +503,7 @@ __device__ __forceinline__ float2 df_voxel_value2(const float4* __restrict__ nod
             const float4 w0 = __ldg(nd), w1 = __ldg(nd + 1), w2 = __ldg(nd + 2), w3 = __ldg(nd + 3);
             const float4 w4 = __ldg(nd + 4), w5 = __ldg(nd + 5), w6 = __ldg(nd + 6), w7 = __ldg(nd + 7);
             const int Lp = __float_as_int(w7.z), Rp = __float_as_int(w7.w);
-            const int L = child_id(Lp), R = child_id(Rp);
+            const int L = child_index(Lp), R = child_index(Rp);
             const int cl = child_count(Lp), cr = child_count(Rp);
             const float2 dl = obb_d2_2<0>(px, py, pz, w0, w1, w2, w3, w4, w5, w6, w7);
             const float2 dr = obb_d2_2<1>(px, py, pz, w0, w1, w2, w3, w4, w5, w6, w7);
@@ -518,7 +513,7 @@ __device__ __forceinline__ float2 df_voxel_value2(const float4* __restrict__ nod
             if (COUNT) n_test += (unsigned long long)(nl + nr);
 #pragma unroll 1
             for (int k = 0; k < nl + nr; ++k) {
-                const int tri = k < nl ? ~L + k : ~R + (k - nl);
+                const int tri = k < nl ? L + k : R + (k - nl);
                 const float2 t = tri_d2_2(px, py, pz, load_tri(tris, tri), best);
                 if (va && t.x < best.x) { best.x = t.x; lim.x = slack_bound(best.x); }
                 if (vb && t.y < best.y) { best.y = t.y; lim.y = slack_bound(best.y); }

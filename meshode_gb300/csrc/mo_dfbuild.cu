@@ -565,8 +565,9 @@ __global__ void k_obb_nodes(const float4* __restrict__ nodes, const int2* __rest
     t[4] = make_float4(L.a2.x, R.a2.x, L.a2.y, R.a2.y);
     t[5] = make_float4(L.a2.z, R.a2.z, -L.e.z, -R.e.z);
     t[6] = make_float4(a3s[0].x, a3s[1].x, a3s[0].y, a3s[1].y);
-    t[7] = make_float4(a3s[0].z, a3s[1].z, __int_as_float(pack_child(ids[0], cnts[0])),
-                       __int_as_float(pack_child(ids[1], cnts[1])));
+    // ids: a node index, or ~first triangle of a bucket (count > 0)
+    t[7] = make_float4(a3s[0].z, a3s[1].z, __int_as_float(pack_child(cnts[0] ? ~ids[0] : ids[0], cnts[0])),
+                       __int_as_float(pack_child(cnts[1] ? ~ids[1] : ids[1], cnts[1])));
 }
 
 // The full grid: one warp per packet of PX x PY x PZ voxels.
