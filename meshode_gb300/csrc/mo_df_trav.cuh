@@ -119,7 +119,7 @@ __device__ __forceinline__ float dotf3(float3 a, float x, float y, float z) {
 constexpr int NODE_F4 = 8;
 constexpr int64_t MAX_TREE_TRIANGLES = (int64_t)1 << 27;  // index << 3 stays an int
 
-// node: the child's node index (count 0), or the bucket's first triangle
+// a child's id: `index` is its node (count 0) or its bucket's first triangle
 __host__ __device__ __forceinline__ int pack_child(int index, int count) { return (index << 3) | count; }
 // bucket size of a packed child (0: internal node)
 __device__ __forceinline__ int child_count(int packed) { return packed & 7; }
