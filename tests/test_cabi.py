@@ -131,6 +131,14 @@ def test_distance_field_entry_points_check_arguments_without_gpu():
     assert lib.mo_df_tree_scratch_bytes(-1, 3) == 0
     assert lib.mo_df_tree_build(None, 10, None, 4, None, None, 0, None, None, None) == L.MO_ERR_INVALID
     assert b"null" in lib.mo_last_error()
+    # child ids are index << 3 | bucket size: at most 2^27 triangles in a tree
+    assert lib.mo_df_tree_build(None, 10, None, (1 << 27) + 1, None, None, 0, None, None, None) == L.MO_ERR_INVALID
+    assert b"too large" in lib.mo_last_error()
+    opt = L.MoDfOptions(L.MO_DF_LBVH, L.MO_PACKET_4x4x2, 0.0)
+    dummy = (ctypes.c_double * 4)()  # never read: the size is refused first
+    p = ctypes.cast(dummy, ctypes.c_void_p)
+    rc = lib.mo_df_build_ex(p, 10, p, (1 << 27) + 1, 64, p, ctypes.byref(opt), None, 0, p, None, None)
+    assert rc == L.MO_ERR_INVALID and b"too large for the LBVH" in lib.mo_last_error()
     assert lib.mo_df_lazy_bytes(1) == 0 and lib.mo_df_lazy_bytes(L.MO_DF_LAZY_MAX_N + 1) == 0
     assert lib.mo_df_lazy_seed(None, 0, None, -1, None, None, None, 0, None) == L.MO_ERR_INVALID
     assert lib.mo_df_lazy_seed(None, 0, None, 0, None, None, None, 0, None) == L.MO_OK  # nothing to seed
